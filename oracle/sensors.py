@@ -1,0 +1,28 @@
+"""Oracle: volumetric heating Q from recorded phasors (NumPy, FP64).
+
+TEST INFRASTRUCTURE ONLY (see :mod:`oracle`). Restates
+``HeatingSource.from_phasors`` (sensors.py:193-295): Q = sum_n alpha_n
+|P_n|^2 / (rho c) in float64, returned as float32.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+def heating_q(phasors: dict, *, alpha, rho, c, harmonics=None, alpha_power_law_y=None):
+    """Q [W/m^3] (sensors.py:259-273); alpha_n = alpha_f0 n^y when y is given (sensors.py:393-402)."""
+    requested = tuple(sorted(phasors)) if harmonics is None else tuple(harmonics)
+    shape = np.shape(phasors[requested[0]])
+    alpha_f0 = np.broadcast_to(np.asarray(alpha, np.float64), shape)
+    rho_map = np.broadcast_to(np.asarray(rho, np.float64), shape)
+    c_map = np.broadcast_to(np.asarray(c, np.float64), shape)
+    if any(n >= 2 for n in requested) and alpha_power_law_y is None:
+        raise ValueError("harmonics above the fundamental need an absorption model")
+    inv_rho_c = 1.0 / (rho_map * c_map)
+    q = np.zeros(shape, dtype=np.float64)
+    for n in requested:
+        a_n = alpha_f0 if alpha_power_law_y is None else alpha_f0 * float(n) ** alpha_power_law_y
+        p2 = np.abs(np.asarray(phasors[n])).astype(np.float64) ** 2
+        q += a_n * p2 * inv_rho_c
+    return np.ascontiguousarray(q, dtype=np.float32)

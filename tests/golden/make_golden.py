@@ -1,0 +1,190 @@
+"""Generate the golden fixtures that pin the oracle to the reference.
+
+Runs the UNCHANGED reference (ebx0/caustica, pure Python) from a source
+checkout on small cases and writes inputs and outputs to ``*.npz`` files
+beside this script. FP64 runs use a backend plugin ``numpy64`` whose array
+module reads ``float32``/``complex64`` as ``float64``/``complex128`` and is
+otherwise NumPy, registered through the reference's own backend registry
+(core/backend.py:44); the engine and the Pennes solver run unmodified.
+
+Usage (needs the reference checkout; the fixtures are committed, so the
+tests themselves never need it)::
+
+    python tests/golden/make_golden.py /path/to/caustica/src
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+
+def _install_numpy64(caustica_backend):
+    class _NumPy64(types.ModuleType):
+        def __getattr__(self, name):
+            if name == "float32":
+                return np.float64
+            if name == "complex64":
+                return np.complex128
+            return getattr(np, name)
+
+    proxy = _NumPy64("numpy64")
+    Backend = caustica_backend.Backend
+
+    def _factory():
+        return Backend("numpy64", proxy)
+
+    _factory.__module__ = __name__
+    _factory.__qualname__ = "numpy64_factory"
+    if "numpy64" not in caustica_backend.backends.available():
+        caustica_backend.backends.register("numpy64")(_factory)
+
+
+def _medium_random(shape, seed, *, beta=0.0):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(1450.0, 1650.0, shape).astype(np.float32)
+    rho = rng.uniform(900.0, 1100.0, shape).astype(np.float32)
+    alpha = rng.uniform(0.0, 30.0, shape).astype(np.float32)
+    b = np.full(shape, beta, np.float32) if beta else np.zeros(shape, np.float32)
+    return alpha, rho, c, b
+
+
+def _random_source(shape, n, seed, margin):
+    rng = np.random.default_rng(seed)
+    pts = set()
+    while len(pts) < n:
+        pts.add(tuple(int(rng.integers(margin, s - margin)) for s in shape))
+    idx = np.array(sorted(pts), np.int64)
+    ph = rng.uniform(-np.pi, np.pi, len(idx)).astype(np.float32)
+    return idx, ph
+
+
+def kspace_case(name, *, shape, dx, pml_vox, seed, n_src, solver, amplitude, f0, spec_kw,
+                harmonics=(1,), record_region=None, reference_point=None, beta=0.0,
+                backend="numpy64", homogeneous=False):
+    from caustica import Grid, Medium, PMLSpec
+    from caustica.solvers import CWRunSpec
+    import caustica.solvers as solvers
+    from caustica.sources import CWSource
+
+    grid = Grid(shape, dx, PMLSpec(pml_vox * dx))
+    if homogeneous:
+        alpha = np.full(shape, 0.5, np.float32)
+        rho = np.full(shape, 1000.0, np.float32)
+        c = np.full(shape, 1500.0, np.float32)
+        b = np.full(shape, beta, np.float32)
+    else:
+        alpha, rho, c, b = _medium_random(shape, seed, beta=beta)
+    med = Medium(alpha=alpha, rho=rho, c=c, beta=b)
+    idx, ph = _random_source(shape, n_src, seed + 1, pml_vox)
+    src = CWSource(indices=idx, phases=ph, amplitude=amplitude, f0=f0)
+    spec = CWRunSpec(**spec_kw)
+    res = solvers.get(solver)().run(
+        grid, med, src, spec, backend=backend, harmonics=harmonics,
+        record_region=record_region, reference_point=reference_point,
+    )
+    out = {
+        "shape": np.array(shape), "dx": dx, "pml_vox": grid.pml_vox, "pml_edge": 2.0,
+        "alpha": alpha, "rho": rho, "c": c, "beta": b,
+        "src_idx": idx, "src_phase": ph, "amplitude": amplitude, "f0": f0, "ramp_periods": 3.0,
+        "nonlinear": solver == "westervelt", "harmonics": np.array(harmonics),
+        "spec": json.dumps(spec_kw),
+        "record_region": json.dumps(None if record_region is None else [[s.start, s.stop] for s in record_region]),
+        "reference_point": json.dumps(None if reference_point is None else list(reference_point)),
+        "spp": res.spp, "dt": res.dt, "steps_total": res.steps_total, "tof_periods": res.tof_periods,
+        "converged_period": res.converged_period, "settle_capped": res.settle_capped,
+        "history": np.array(res.convergence_history, np.float64).reshape(-1, 3),
+        "p_max": res.p_max,
+        "region": np.array([[s.start, s.stop] for s in res.region]),
+    }
+    for h in harmonics:
+        out[f"phasor_h{h}"] = res.phasors[h]
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(f"{name}: spp={res.spp} steps={res.steps_total} |P|max={np.abs(res.phasor).max():.4g}")
+
+
+def pennes_case(name, *, shape, dx, seed, dt, n_steps, boundary="insulated", on_unstable="refuse",
+                q_scale=2e6, perfused=True, chain_steps=0, reference_temperature_c=None):
+    from caustica.thermal import PennesSolver, ThermalMedium
+
+    rng = np.random.default_rng(seed)
+    k = rng.uniform(0.3, 0.6, shape).astype(np.float32)
+    rho = rng.uniform(950.0, 1100.0, shape).astype(np.float32)
+    cp = rng.uniform(3000.0, 4000.0, shape).astype(np.float32)
+    w = (rng.uniform(0.0, 0.02, shape) if perfused else np.zeros(shape)).astype(np.float32)
+    tmed = ThermalMedium(k=k, rho=rho, specific_heat=cp, perfusion=w, dx=dx)
+    q = (rng.random(shape) ** 4 * q_scale).astype(np.float32)
+    t0 = (37.0 + rng.uniform(0.0, 2.0, shape)).astype(np.float32)
+    solver = PennesSolver("numpy64", boundary=boundary, on_unstable=on_unstable,
+                          reference_temperature_c=reference_temperature_c)
+    hot = solver.solve(t0, q, tmed, dt=dt, n_steps=n_steps, dose=True, record_every=max(1, n_steps // 3))
+    out = {
+        "shape": np.array(shape), "dx": dx, "dt": dt, "n_steps": n_steps, "k": k, "rho": rho, "cp": cp,
+        "w": w, "q": q, "t0": t0, "boundary": boundary, "on_unstable": on_unstable,
+        "reference_temperature_c": json.dumps(reference_temperature_c),
+        "T": hot.temperature, "Tmax": hot.temperature_max, "dose": hot.dose_cem43,
+        "substeps": hot.substeps, "dt_stable": hot.meta["dt_stable_s"],
+        "samples": np.array(hot.samples), "times": np.array(hot.times),
+    }
+    if chain_steps:
+        cool = solver.solve(hot.temperature, None, tmed, dt=dt, n_steps=chain_steps, dose=True,
+                            dose0=hot.dose_cem43)
+        out.update({"chain_steps": chain_steps, "T2": cool.temperature, "Tmax2": cool.temperature_max,
+                    "dose2": cool.dose_cem43})
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(f"{name}: substeps={hot.substeps} Tmax={hot.peak_temperature_c:.4f} dose={hot.peak_dose_cem43:.4g}")
+
+
+def bowl_source_case():
+    """The 500 kHz bowl of the 96x96x128 workload, as the reference voxelises it."""
+    from caustica import Grid, PMLSpec
+    from caustica.sources import bowl_cw_source
+
+    grid = Grid((96, 96, 128), 0.3e-3, PMLSpec(3.0e-3))
+    src = bowl_cw_source(grid, f0=5e5, amplitude=1e5, aperture_radius=12e-3, roc=30e-3, apex_vox=(48, 48, 10))
+    np.savez_compressed(HERE / "bowl_96x96x128.npz", indices=src.indices.astype(np.int16))
+    print(f"bowl: {src.n_points} voxels")
+
+
+def main(src_path: str) -> None:
+    sys.path.insert(0, src_path)
+    import caustica.core.backend as cb
+
+    _install_numpy64(cb)
+    common = dict(f0=1.0e6)
+    kspace_case("ks3d_linear_hetero", shape=(12, 10, 16), dx=0.3e-3, pml_vox=2, seed=11, n_src=14,
+                solver="linear", amplitude=1e5,
+                spec_kw=dict(convergence_tol=0.0, min_settle_periods=2, max_settle_periods=4,
+                             n_record_periods=2), **common)
+    kspace_case("ks3d_westervelt_padded", shape=(7, 11, 13), dx=0.3e-3, pml_vox=1, seed=21, n_src=9,
+                solver="westervelt", amplitude=2e6, beta=4.5, harmonics=(1, 2, 3),
+                record_region=(slice(1, 6), slice(2, None), slice(-9, -1)), reference_point=(3, 5, 10),
+                spec_kw=dict(cfl=0.3, convergence_tol=0.0, min_settle_periods=3, max_settle_periods=3,
+                             n_record_periods=1), **common)
+    kspace_case("ks1d_plane_converge", shape=(96,), dx=0.375e-3, pml_vox=12, seed=31, n_src=1,
+                solver="linear", amplitude=1e5, homogeneous=True,
+                spec_kw=dict(min_settle_periods=6, max_settle_periods=60, convergence_tol=0.01,
+                             n_record_periods=2), **common)
+    kspace_case("ks2d_westervelt", shape=(20, 24), dx=0.2e-3, pml_vox=3, seed=41, n_src=10,
+                solver="westervelt", amplitude=1.5e6, beta=3.5, harmonics=(1, 2),
+                spec_kw=dict(cfl=0.4, convergence_tol=0.0, min_settle_periods=2, max_settle_periods=3,
+                             n_record_periods=2, t_end_min_us=9.0), **common)
+    kspace_case("ks3d_fp32_reference", shape=(10, 9, 12), dx=0.3e-3, pml_vox=2, seed=51, n_src=8,
+                solver="linear", amplitude=1e5, backend="numpy",
+                spec_kw=dict(convergence_tol=0.0, min_settle_periods=2, max_settle_periods=2,
+                             n_record_periods=1), **common)
+    pennes_case("pennes3d_insulated", shape=(8, 9, 10), dx=0.3e-3, seed=61, dt=0.01, n_steps=40,
+                chain_steps=30)
+    pennes_case("pennes2d_dirichlet_substep", shape=(12, 10), dx=0.25e-3, seed=71, dt=0.2, n_steps=12,
+                boundary="dirichlet", on_unstable="substep", reference_temperature_c=36.0)
+    bowl_source_case()
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
