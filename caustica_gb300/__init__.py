@@ -1,0 +1,28 @@
+"""caustica_gb300 -- GB300-native (sm_103a) k-space CW solver and Pennes/CEM43 step.
+
+A drop-in for caustica's ``linear``/``westervelt`` solvers and its
+``PennesSolver``: the host code here mirrors the reference interfaces and
+calls ``libcaustica_gb300.so`` (C ABI, ``include/caustica_gb300.h``) through
+ctypes. Every time step runs in hand-written CUDA kernels; there is no CPU
+fallback.
+"""
+
+from .contract import (
+    CWRunSpec,
+    CWSource,
+    Grid,
+    Medium,
+    PMLSpec,
+    SolverCapabilityError,
+    SolverDivergedError,
+    SolverResult,
+)
+from .solvers import LinearKSpaceGB300, WesterveltKSpaceGB300, get
+from .thermal import PennesSolverGB300, ThermalMedium, ThermalResult
+
+__all__ = [
+    "CWRunSpec", "CWSource", "Grid", "Medium", "PMLSpec", "SolverCapabilityError", "SolverDivergedError",
+    "SolverResult", "LinearKSpaceGB300", "WesterveltKSpaceGB300", "get", "PennesSolverGB300", "ThermalMedium",
+    "ThermalResult",
+]
+__version__ = "0.1.0"

@@ -1,0 +1,143 @@
+"""ctypes binding of ``libcaustica_gb300.so`` (the C ABI in ``include/caustica_gb300.h``).
+
+The library is the only compute path: if it is missing or cannot be loaded
+the import of anything that needs it raises. There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libcaustica_gb300.so"
+
+CG_OK = 0
+CG_ERR_INVALID = 1
+CG_ERR_OOM = 2
+CG_ERR_CUDA = 3
+CG_ERR_NONFINITE = 4
+CG_ERR_TIMEOUT = 5
+
+
+class CGError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code: int, func: str, msg: str):
+        super().__init__(f"{func} failed (code {code}): {msg}")
+        self.code = code
+
+
+class CGInvalidArgument(CGError, ValueError):
+    """The library refused its arguments (CG_ERR_INVALID)."""
+
+
+class SolverConfig(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("batch", C.c_int), ("nonlinear", C.c_int), ("spp", C.c_int), ("max_periods", C.c_int),
+        ("n_harmonics", C.c_int), ("harmonics", C.c_int * 8),
+        ("pml", C.c_int * 3), ("pml_edge", C.c_double),
+        ("dx", C.c_double), ("dt", C.c_double), ("c_ref", C.c_double),
+        ("rec_lo", C.c_int * 3), ("rec_hi", C.c_int * 3),
+        ("conv_lo", C.c_int * 3), ("conv_hi", C.c_int * 3),
+    ]
+
+
+class PennesConfig(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("dirichlet", C.c_int), ("dose", C.c_int),
+        ("theta_wall", C.c_float), ("t_ref", C.c_float), ("half_dt_min", C.c_float),
+        ("n_labels", C.c_int),
+    ]
+
+
+_P = C.c_void_p
+_I = C.c_int
+_LL = C.c_longlong
+
+# name -> (argtypes); every function returns int unless listed in _RESTYPE
+SIGNATURES = {
+    "cg_last_error": [],
+    "cg_version": [],
+    "cg_solver_create": [C.POINTER(SolverConfig), C.POINTER(_P)],
+    "cg_solver_destroy": [_P],
+    "cg_solver_set_medium_labels": [_P, _P, _I, _P],
+    "cg_solver_set_medium_dense": [_P, _P, _P, _P, _P],
+    "cg_solver_set_source": [_P, _I, _P, _P, _P],
+    "cg_solver_set_drive": [_P, _I, _P],
+    "cg_solver_reset": [_P],
+    "cg_solver_run": [_P, _I, _I],
+    "cg_solver_run_periods": [_P, _I, _I],
+    "cg_solver_begin_record": [_P],
+    "cg_solver_read_peaks": [_P, _I, _I, _P],
+    "cg_solver_finalize": [_P, _I, _P, _P],
+    "cg_solver_get_state": [_P, _P, _P],
+    "cg_solver_set_state": [_P, _P, _P, _LL],
+    "cg_solver_synchronize": [_P],
+    "cg_solver_info": [_P, _P],
+    "cg_solver_timed_run": [_P, _I, _I, _I, _P],
+    "cg_solver_profile": [_P, _I, _I, _P],
+    "cg_fft3d_create": [_I, _I, _I, _I, C.POINTER(_P)],
+    "cg_fft3d_destroy": [_P],
+    "cg_fft3d_forward": [_P, _P, _P],
+    "cg_fft3d_inverse": [_P, _P, _P],
+    "cg_pennes_create": [C.POINTER(PennesConfig), C.POINTER(_P)],
+    "cg_pennes_destroy": [_P],
+    "cg_pennes_set_coefficients": [_P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "cg_pennes_set_state": [_P, _P, _P, _P],
+    "cg_pennes_run": [_P, _I],
+    "cg_pennes_check_finite": [_P, _P],
+    "cg_pennes_get_state": [_P, _P, _P, _P],
+}
+_RESTYPE = {"cg_last_error": C.c_char_p}
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load the library (once) and declare every exported signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(
+            f"{p} is missing: build it with `python -m caustica_gb300.build` "
+            f"(there is no CPU fallback for this solver)"
+        )
+    lib = C.CDLL(str(p))
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPE.get(name, C.c_int)
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().cg_last_error().decode(errors="replace")
+
+
+def check(code: int, func: str) -> None:
+    if code != CG_OK:
+        msg = last_error()
+        if code == CG_ERR_INVALID:
+            raise CGInvalidArgument(code, func, msg)
+        raise CGError(code, func, msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args), name)
+
+
+def ptr(a: np.ndarray | None):
+    """Host pointer of a C-contiguous array (None -> NULL)."""
+    if a is None:
+        return None
+    if not a.flags.c_contiguous:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(C.c_void_p)

@@ -1,0 +1,68 @@
+"""One and several bare steps of the fused kernels against the oracle's step (GPU)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from caustica_gb300 import contract as ct
+from caustica_gb300 import engine as eng
+from oracle import kspace as ok
+
+pytestmark = pytest.mark.gpu
+
+CASES = [((12, 10, 16), False, True), ((9, 12, 10), True, True), ((16, 16, 24), True, False), ((1, 1, 40), False, True),
+         ((1, 18, 20), True, True), ((48, 40, 64), True, True)]
+
+
+def _setup(shape, nonlinear, hetero, seed=0):
+    rng = np.random.default_rng(seed)
+    if hetero:
+        c = rng.uniform(1450, 1650, shape).astype(np.float32)
+        rho = rng.uniform(900, 1100, shape).astype(np.float32)
+        alpha = rng.uniform(0, 40, shape).astype(np.float32)
+    else:
+        c = np.full(shape, 1500, np.float32)
+        rho = np.full(shape, 1000, np.float32)
+        alpha = np.full(shape, 2.0, np.float32)
+    beta = np.full(shape, 4.5 if nonlinear else 0.0, np.float32)
+    nd3 = [n for n in shape if n > 1] if shape[0] == 1 else list(shape)
+    gshape = tuple(nd3)
+    grid = ct.Grid(gshape, 0.25e-3, ct.PMLSpec(2 * 0.25e-3))
+    med = ct.Medium(alpha.reshape(gshape), rho.reshape(gshape), c.reshape(gshape), beta.reshape(gshape))
+    idx = np.array([[n // 2 for n in gshape]], np.int64)
+    src = ct.CWSource(indices=idx, phases=np.zeros(1, np.float32), amplitude=1e5, f0=1e6)
+    spec = ct.CWRunSpec(cfl=0.3)
+    plan = eng.make_plan("step", grid, med, src, spec, nonlinear=nonlinear)
+    return plan, grid, med, rng
+
+
+@pytest.mark.parametrize("shape,nonlinear,hetero", CASES)
+def test_steps_match_the_oracle_step(shape, nonlinear, hetero):
+    plan, grid, med, rng = _setup(shape, nonlinear, hetero)
+    p0 = (rng.standard_normal(plan.padded) * 1e5).astype(np.float32)
+    u0 = [(rng.standard_normal(plan.padded) * 0.05).astype(np.float32) for _ in range(plan.nd)]
+    nsteps = 3
+    with eng.DeviceSolver(plan) as dev:
+        u3 = np.zeros((3, 1, plan.ncell), np.float32)
+        for i in range(plan.nd):
+            u3[3 - plan.nd + i, 0] = u0[i].reshape(-1)
+        dev.set_state(p0.reshape(1, -1), u3, 0)
+        # the source ramp is exactly zero at t = 0, so step 0 injects nothing
+        dev.run_steps(1)
+        p1, u1 = dev.get_state()
+    maps = ok.medium_maps(med.alpha, med.rho, med.c, med.beta, plan.padded, plan.dt, nonlinear, np.float64)
+    ks = ok.k_vectors(plan.padded, plan.dx, np.float64)
+    kap = ok.kappa_sinc(ks, plan.c_max, plan.dt, np.float64)
+    der = ok.spectral_derivative_factors(ks, kap, plan.padded, np.complex128)
+    spg = ok.sponge_volume(plan.padded, grid.pml_vox, 2.0, np.float64)
+    pr = p0.astype(np.float64)
+    ur = [x.astype(np.float64) for x in u0]
+    pr, ur = ok.step_fields(p=pr, u=ur, dt_over_rho=maps[0], rhoc2_dt=maps[1], absorb=maps[2], beta2_dt=maps[3],
+                            sponge=spg, deriv=der, padded=plan.padded)
+    gp = p1[0].reshape(plan.padded)
+    assert np.abs(gp - pr).max() / np.abs(pr).max() < 2e-6
+    for i in range(plan.nd):
+        gu = u1[3 - plan.nd + i, 0].reshape(plan.padded)
+        assert np.abs(gu - ur[i]).max() / np.abs(ur[i]).max() < 2e-6
+    del nsteps

@@ -1,0 +1,82 @@
+"""Pennes + CEM43 on the GPU against the reference's goldens and its float32 path (GPU)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import PENNES_GOLDEN, load_golden
+import caustica_gb300 as cg
+from oracle import pennes as op
+
+pytestmark = pytest.mark.gpu
+
+T_TOL = 1e-3  # K, max-abs
+DOSE_TOL = 1e-3  # relative
+
+
+def _solve(g, **kw):
+    tm = cg.ThermalMedium(g["k"], g["rho"], g["cp"], g["w"], g["dx"])
+    s = cg.PennesSolverGB300(boundary=g["boundary"], on_unstable=g["on_unstable"],
+                             reference_temperature_c=g["reference_temperature_c"])
+    return s, tm, s.solve(g["t0"], g["q"], tm, dt=g["dt"], n_steps=g["n_steps"], dose=True,
+                          record_every=max(1, g["n_steps"] // 3), **kw)
+
+
+@pytest.mark.parametrize("name", PENNES_GOLDEN)
+def test_pennes_matches_reference_fp64(name):
+    g = load_golden(name)
+    s, tm, res = _solve(g)
+    assert res.substeps == g["substeps"]
+    assert np.abs(res.temperature - g["T"]).max() < T_TOL
+    assert np.abs(res.temperature_max - g["Tmax"]).max() < T_TOL
+    rel = np.abs(res.dose_cem43 - g["dose"]) / np.maximum(np.abs(g["dose"]), 1e-30)
+    assert rel.max() < DOSE_TOL
+    assert len(res.samples) == len(g["samples"])
+    if "chain_steps" in g:
+        cool = s.solve(res.temperature, None, tm, dt=g["dt"], n_steps=g["chain_steps"], dose=True,
+                       dose0=res.dose_cem43)
+        assert np.abs(cool.temperature - g["T2"]).max() < T_TOL
+        rel2 = np.abs(cool.dose_cem43 - g["dose2"]) / np.abs(g["dose2"])
+        assert rel2.max() < DOSE_TOL
+        chained = cg.ThermalResult.chain([res, cool])
+        assert chained.n_steps == g["n_steps"] + g["chain_steps"]
+
+
+@pytest.mark.parametrize("name", PENNES_GOLDEN)
+def test_temperature_equals_the_reference_float32_path_bit_for_bit(name):
+    g = load_golden(name)
+    _, _, res = _solve(g)
+    ref = op.solve(g["t0"], g["q"], k=g["k"], rho=g["rho"], specific_heat=g["cp"], perfusion=g["w"], dx=g["dx"],
+                   dt=g["dt"], n_steps=g["n_steps"], dose=True, boundary=g["boundary"],
+                   on_unstable=g["on_unstable"], reference_temperature_c=g["reference_temperature_c"],
+                   dtype=np.float32)
+    np.testing.assert_array_equal(res.temperature, ref["temperature"])
+    np.testing.assert_array_equal(res.temperature_max, ref["temperature_max"])
+
+
+def test_cem43_unit_definitions_on_the_device():
+    """43 C held for 60 s accrues exactly 1 CEM43 minute; 44 C, 2; 42 C, 0.25."""
+    shape = (2, 2, 2)
+    tm = cg.ThermalMedium.homogeneous(shape, k=1e-12, rho=1000.0, specific_heat=4000.0, perfusion=0.0, dx=1e-3)
+    for temp, want in ((43.0, 1.0), (44.0, 2.0), (42.0, 0.25)):
+        res = cg.PennesSolverGB300().solve(np.full(shape, temp, np.float32), None, tm, dt=1.0, n_steps=60, dose=True)
+        np.testing.assert_allclose(res.dose_cem43, want, rtol=1e-6)
+
+
+def test_a_state_that_stops_being_finite_raises_instead_of_returning_nan():
+    """A near-insulator with a heat source float32 cannot carry (the reference's own recipe)."""
+    shape = (8, 8, 8)
+    tm = cg.ThermalMedium.homogeneous(shape, k=1e-6, rho=1050.0, specific_heat=3600.0, perfusion=0.0, dx=1e-3)
+    s = cg.PennesSolverGB300()
+    with pytest.raises(cg.thermal.ThermalDivergedError) as exc:
+        s.solve(np.full(shape, 37.0, np.float32), 1e37, tm, s.stable_dt(tm), 300)
+    msg = str(exc.value)
+    assert "stopped being finite" in msg and "outer step" in msg and "stable_dt" in msg
+
+
+def test_an_overflowing_dose_is_caught_by_the_same_guard():
+    shape = (4, 4, 4)
+    tm = cg.ThermalMedium.homogeneous(shape, k=0.5, rho=1050.0, specific_heat=3600.0, perfusion=0.0, dx=1e-3)
+    with pytest.raises(cg.thermal.ThermalDivergedError, match="CEM43 dose"):
+        cg.PennesSolverGB300().solve(np.full(shape, 37.0, np.float32), 2.0e6, tm, 1.0, 400, dose=True)
