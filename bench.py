@@ -1,0 +1,371 @@
+"""Benchmark: Westervelt CW solve on 192x192x256 (harmonics 1-3) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One "step" is one time step of the k-space solver over the whole grid
+(9,437,184 cells, labelled four-tissue medium, 10,862 source voxels). The
+metric is grid-cell-steps/s (cells x steps / device time), whole job over
+all ranks. Inputs are larger than L2 between timed steps (p and u are
+151 MB, the three spectra 114 MB; L2 is 129 MB), so no flush is needed.
+
+gb300 arm (default): K steps timed with CUDA events on the solver's stream,
+barrier + synchronise on both sides, max over ranks; plus the per-launch
+profile and roofline of the dominant kernel, a full end-to-end solve
+through the public solver front from host numpy inputs (``e2e``), and the
+reference CPU path timed on a bounded sample (``cpu_baseline``).
+
+reference arm (``--impl reference``): the reference's CPU path for this step
+(the NumPy/SciPy restatement in ``oracle/``, float32 like the reference's
+stock path, all host cores) timed on a bounded sample of the same workload.
+Under torchrun only rank 0 runs it.
+
+N > 1: one process per GPU (torchrun), each rank solving its own replica of
+the workload; ``scaling`` is "weak" and there is no data-path collective.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import signal
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "grid-cell-steps/s"
+UNIT = "cell-steps/s"
+LABEL_BYTES = 1  # uint8 material label per cell
+
+
+def _jsonable(o):
+    if isinstance(o, np.generic):
+        return o.item()
+    raise TypeError(f"not JSON serialisable: {type(o).__name__}")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        return dist, rank, ws, local
+    return None, 0, 1, 0
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (SM clock, limits, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int, path: Path | None = None):
+        self.index = index
+        self.proc = None
+        self.path = path or Path(os.environ.get("TMPDIR", "/tmp")) / f"cg_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        exe = shutil.which("nvidia-smi")
+        if exe:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen([exe, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "100"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.send_signal(signal.SIGTERM)
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        # samples under load: the upper half of SM clock readings
+        load = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": float(np.median(load)) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(rows), "reasons": reasons}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, or None."""
+    f = ROOT / "profiles" / "traffic_per_launch.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+SLOTS = ["k_ypass:fwd", "k_xpass:grad", "k_ypass:inv_grad", "k_zpass_u", "k_ypass:fwd_div", "k_xpass:div",
+         "k_ypass:inv", "k_zpass_p"]
+
+
+def slot_bytes(ncell: int, nspec: int, labels: bool, nonlinear: bool, record: bool = False) -> list[int]:
+    """Algorithmic bytes per launch of each slot: every input read once and
+    every output written once in the kernel's own layout."""
+    c8 = 8 * nspec
+    r4 = 4 * ncell
+    maps_u = LABEL_BYTES * ncell if labels else 8 * ncell
+    maps_p = LABEL_BYTES * ncell if labels else (12 if nonlinear else 8) * ncell
+    rec = 6 * r4 if record else 0
+    return [2 * c8, 3 * c8, 5 * c8, 6 * c8 + 6 * r4 + maps_u, 5 * c8, 3 * c8, 2 * c8, 2 * c8 + 2 * r4 + maps_p + rec]
+
+
+def step_algorithmic_bytes(labels: bool, nonlinear: bool) -> int:
+    """Compulsory bytes per cell-step of the whole step (all passes fused):
+    80 / 84 B with float32 maps, 66 B with label-indexed maps."""
+    if labels:
+        return 66
+    return 84 if nonlinear else 80
+
+
+def cpu_sample(job, target_s: float = 12.0, workers: int | None = None):
+    """Time the reference's float32 NumPy step (oracle restatement) on this host."""
+    from caustica_gb300 import engine as eng
+    from oracle import kspace as ok
+
+    workers = workers or os.cpu_count() or 1
+    grid, med, src, spec = job["grid"], job["medium"], job["source"], job["spec"]
+    shape = grid.shape
+    spp, dt = eng.cw_discretization(grid.dx, float(med.c.max()), src.f0, spec, job["harmonics"])
+    maps = ok.medium_maps(med.alpha, med.rho, med.c, med.beta, shape, dt, job["nonlinear"], np.float32)
+    ks = ok.k_vectors(shape, grid.dx, np.float32)
+    kap = ok.kappa_sinc(ks, float(med.c.max()), dt, np.float32)
+    der = ok.spectral_derivative_factors(ks, kap, shape, np.complex64)
+    spg = ok.sponge_volume(shape, grid.pml_vox, 2.0, np.float32)
+    rng = np.random.default_rng(0)
+    p = (rng.standard_normal(shape) * 1e3).astype(np.float32)
+    u = [np.zeros(shape, np.float32) for _ in range(3)]
+    import scipy.fft as spfft
+
+    n = 0
+    t0 = time.perf_counter()
+    with spfft.set_workers(workers):
+        while True:
+            ok.step_fields(p=p, u=u, dt_over_rho=maps[0], rhoc2_dt=maps[1], absorb=maps[2], beta2_dt=maps[3],
+                           sponge=spg, deriv=der, padded=shape)
+            n += 1
+            el = time.perf_counter() - t0
+            if el >= target_s or n >= 200:
+                break
+    cells = int(np.prod(shape))
+    return {"value": cells * n / el, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{n} float32 NumPy/SciPy steps of the {shape[0]}x{shape[1]}x{shape[2]} Westervelt step "
+                      f"({el:.1f} s, scipy.fft workers={workers})", "steps": n, "seconds": el}
+
+
+def run_reference(args, dist, rank):
+    from caustica_gb300 import workloads as wl
+
+    if rank != 0:
+        return
+    job = wl.config2()
+    budget = float(os.environ.get("CG_REFERENCE_SECONDS", "45"))
+    # warm-up: one step (plans and page faults), then a bounded sample
+    cpu_sample(job, target_s=0.0)
+    s = cpu_sample(job, target_s=budget)
+    line = {"impl": "reference", "metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": s["steps"], "warmup": 1, "ms_per_step": 1e3 * s["seconds"] / s["steps"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": job["name"], "grid": list(job["grid"].shape), "harmonics": list(job["harmonics"]),
+                       "l2": "inputs larger than L2"},
+            "cpu_baseline": {k: s[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": s["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line, default=_jsonable), flush=True)
+
+
+def run_gb300(args, dist, rank, ws, local):
+    from caustica_gb300 import _lib
+    from caustica_gb300 import engine as eng
+    from caustica_gb300 import workloads as wl
+    from caustica_gb300.solvers import WesterveltKSpaceGB300
+
+    _lib.load()
+    _lib.call("cg_set_device", local)
+    job = wl.config2()
+    grid, med, src, spec = job["grid"], job["medium"], job["source"], job["spec"]
+    plan = eng.make_plan("westervelt_gb300", grid, med, src, spec, nonlinear=True, harmonics=job["harmonics"],
+                         reference_point=job["reference_point"])
+    ncell = plan.ncell
+    K, W = int(args.steps), int(args.warmup)
+    graph = K % plan.spp == 0 and W % plan.spp == 0
+    dev = eng.DeviceSolver(plan)
+    try:
+        # drive table long enough that the source keeps injecting through the timed steps
+        dev.extend_drive((plan.eff_min + 4) * plan.spp + W + 2 * K)
+        # run far enough to have a developed field, then warm up
+        pre = plan.eff_min if args.prerun_periods is None else int(args.prerun_periods)
+        dev.run_periods(pre)
+        ms = C_float()
+        if W:
+            _lib.call("cg_solver_timed_run", dev.h, W, 0, int(graph), ms.ref())
+        dev.synchronize()
+        _barrier(dist)
+        with Clocks(local) as clk:
+            _lib.call("cg_solver_timed_run", dev.h, K, 0, int(graph), ms.ref())
+        dev.synchronize()
+        _barrier(dist)
+        t_ms = _max_over_ranks(dist, ms.value)
+        value = ws * ncell * K / (t_ms * 1e-3)
+        # per-launch profile (events between launches)
+        prof = np.zeros(8, np.float32)
+        P = 2 * plan.spp
+        _lib.call("cg_solver_profile", dev.h, P, 0, _lib.ptr(prof))
+    finally:
+        dev.close()
+
+    hbm, peak_kind = _peaks()
+    info_labels = plan.labels is not None
+    nspec = plan.padded3[0] * (plan.padded3[2] // 2 + 1) * plan.padded3[1]
+    bytes_slot = slot_bytes(ncell, nspec, info_labels, True)
+    per_launch_ms = prof / P
+    dom = int(np.argmax(per_launch_ms))
+    achieved = bytes_slot[dom] / (per_launch_ms[dom] * 1e-3) / 1e9
+    kernel_name = SLOTS[dom]
+    traffic = _traffic_from_profiles(kernel_name)
+    step_b = step_algorithmic_bytes(info_labels, True)
+    step_achieved = step_b * value / ws / 1e9
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": t_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": job["name"], "grid": list(plan.padded3), "cells": ncell,
+                       "harmonics": list(plan.harmonics), "medium": f"{len(plan.label_table)} labels (uint8 map)",
+                       "source_voxels": int(plan.src_xyz.shape[0]), "spp": plan.spp,
+                       "timing": "CUDA events on the solver stream, " + ("CUDA graph per period" if graph else
+                                                                           "direct launches"),
+                       "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush"},
+            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_launch": bytes_slot[dom],
+                         "ms_per_launch": float(per_launch_ms[dom]), "traffic": traffic},
+            "step_roofline": {"bytes_per_cell_step": step_b, "achieved": step_achieved, "peak": hbm,
+                              "frac": step_achieved / hbm, "unit": "GB/s",
+                              "note": "algorithmic bytes of the fully fused step with label-indexed maps"},
+            "profile_ms_per_launch": {SLOTS[i]: float(per_launch_ms[i]) for i in range(8)},
+            "gpu_launches": K * 8 + (K // plan.spp if graph else 1)}
+
+    # end-to-end: one full solve through the public solver front, host numpy in, host numpy out
+    if not args.skip_e2e:
+        solver = WesterveltKSpaceGB300()
+        solver.run(grid, med, src, spec, harmonics=job["harmonics"], reference_point=job["reference_point"])
+        _barrier(dist)
+        t0 = time.perf_counter()
+        res = solver.run(grid, med, src, spec, harmonics=job["harmonics"], reference_point=job["reference_point"])
+        el = _max_over_ranks(dist, time.perf_counter() - t0)
+        h2d = (plan.labels.nbytes + plan.label_table.nbytes + plan.src_xyz.nbytes + 8 * plan.src_xyz.shape[0]
+               + 16 * plan.max_periods * plan.spp)
+        d2h = sum(v.nbytes for v in res.phasors.values()) + res.p_max.nbytes
+        e2e_value = ws * ncell * res.steps_total / el
+        line["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "step": f"one full solve ({res.steps_total} time steps, {res.steps_total // plan.spp} periods) "
+                               f"through WesterveltKSpaceGB300.run() from host numpy",
+                       "seconds": el, "solves_per_s": ws / el}
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        cb = cpu_sample(job, target_s=float(os.environ.get("CG_CPU_SECONDS", "12")))
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line["clocks"] = clk.summary()
+    if rank == 0:
+        print(json.dumps(line, default=_jsonable), flush=True)
+
+
+class C_float:
+    def __init__(self):
+        import ctypes
+
+        self._v = ctypes.c_float(0.0)
+
+    def ref(self):
+        import ctypes
+
+        return ctypes.byref(self._v)
+
+    @property
+    def value(self):
+        return float(self._v.value)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4400)
+    ap.add_argument("--warmup", type=int, default=44)
+    ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--prerun-periods", type=int, default=None,
+                    help="periods run before the warm-up (default: the settle floor of the workload)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    dist, rank, ws, local = _dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist, rank)
+        else:
+            run_gb300(args, dist, rank, ws, local)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

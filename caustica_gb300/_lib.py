@@ -63,6 +63,7 @@ _LL = C.c_longlong
 SIGNATURES = {
     "cg_last_error": [],
     "cg_version": [],
+    "cg_set_device": [_I],
     "cg_solver_create": [C.POINTER(SolverConfig), C.POINTER(_P)],
     "cg_solver_destroy": [_P],
     "cg_solver_set_medium_labels": [_P, _P, _I, _P],

@@ -45,6 +45,11 @@ void cg_set_error(const char* fmt, ...) {
 extern "C" const char* cg_last_error(void) { return g_err; }
 extern "C" int cg_version(void) { return 10000; }
 
+extern "C" int cg_set_device(int device) {
+  CG_CUDA_TRY(cudaSetDevice(device));
+  return CG_OK;
+}
+
 // ------------------------------------------------------------ structures --
 #define CG_TILE 16   // pencils per tile
 #define CG_ZROWS 32  // real rows per z tile (two per complex pencil)
@@ -898,8 +903,6 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
   ALLOC(s->sx, cfg->nx);
   ALLOC(s->sy, cfg->ny);
   ALLOC(s->sz, cfg->nz);
-  ALLOC(s->bins, B * s->spp * s->nrec);
-  ALLOC(s->comp, B * s->spp * s->nrec);
   ALLOC(s->pmax, B * s->nrec);
   ALLOC(s->peaks, B * s->max_periods);
   ALLOC(s->harm_dev, CG_MAX_H);
@@ -1133,6 +1136,7 @@ static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = 
 
 extern "C" int cg_solver_run(cg_solver* s, int n_steps, int record) {
   CG_REQUIRE(s, "null solver");
+  CG_REQUIRE(!record || s->bins, "recording needs cg_solver_begin_record first");
   CG_REQUIRE(s->has_medium, "set a medium before running");
   CG_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
   for (int i = 0; i < n_steps; ++i) launch_step(s, i, record);
@@ -1143,6 +1147,7 @@ extern "C" int cg_solver_run(cg_solver* s, int n_steps, int record) {
 
 extern "C" int cg_solver_run_periods(cg_solver* s, int n_periods, int record) {
   CG_REQUIRE(s, "null solver");
+  CG_REQUIRE(!record || s->bins, "recording needs cg_solver_begin_record first");
   CG_REQUIRE(s->has_medium, "set a medium before running");
   CG_REQUIRE(n_periods >= 0, "n_periods must be >= 0");
   const int gi = record ? 1 : 0;
@@ -1171,6 +1176,13 @@ extern "C" int cg_solver_run_periods(cg_solver* s, int n_periods, int record) {
 extern "C" int cg_solver_begin_record(cg_solver* s) {
   CG_REQUIRE(s, "null solver");
   const size_t nb = (size_t)s->B * s->spp * s->nrec;
+  // the phase-bin accumulators exist only from the first record window on
+  if (!s->bins) {
+    invalidate_graphs(s);
+    int rc = dev_alloc(&s->bins, nb);
+    if (rc == CG_OK) rc = dev_alloc(&s->comp, nb);
+    if (rc != CG_OK) return rc;
+  }
   CG_CUDA_TRY(cudaMemsetAsync(s->bins, 0, sizeof(float) * nb, s->stream));
   CG_CUDA_TRY(cudaMemsetAsync(s->comp, 0, sizeof(float) * nb, s->stream));
   CG_CUDA_TRY(cudaMemsetAsync(s->pmax, 0, sizeof(float) * (size_t)s->B * s->nrec, s->stream));
@@ -1189,6 +1201,7 @@ extern "C" int cg_solver_read_peaks(cg_solver* s, int first, int count, float* o
 
 extern "C" int cg_solver_finalize(cg_solver* s, int n_record_steps, float* phasors, float* pmax) {
   CG_REQUIRE(s, "null solver");
+  CG_REQUIRE(s->bins, "no record window has run (call cg_solver_begin_record first)");
   CG_REQUIRE(n_record_steps >= 1, "n_record_steps must be >= 1");
   float2* out = nullptr;
   int rc = dev_alloc(&out, (size_t)s->B * s->nh * s->nrec);
@@ -1276,6 +1289,7 @@ extern "C" int cg_solver_timed_run(cg_solver* s, int n_steps, int record, int gr
 // the step, in step order), events recorded between launches.
 extern "C" int cg_solver_profile(cg_solver* s, int n_steps, int record, float* ms8) {
   CG_REQUIRE(s && ms8, "null argument");
+  CG_REQUIRE(!record || s->bins, "recording needs cg_solver_begin_record first");
   cudaEvent_t ev[9];
   for (int i = 0; i < 9; ++i) CG_CUDA_TRY(cudaEventCreate(&ev[i]));
   for (int i = 0; i < 8; ++i) ms8[i] = 0.f;

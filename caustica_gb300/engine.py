@@ -111,6 +111,21 @@ def material_coefficients(alpha, rho, c, beta, dt, nonlinear_active):
     return dtr, rc2, ab, b2
 
 
+def _first_occurrence(inv: np.ndarray, n: int, chunk: int = 1 << 20) -> np.ndarray:
+    """Index of the first element equal to each label 0..n-1 (chunked scan)."""
+    first = np.full(n, -1, np.int64)
+    missing = n
+    for s0 in range(0, inv.size, chunk):
+        part = inv[s0:s0 + chunk]
+        for lab in np.flatnonzero(np.bincount(part, minlength=n)[:n] > 0):
+            if first[lab] < 0:
+                first[lab] = s0 + int(np.argmax(part == lab))
+                missing -= 1
+        if missing == 0:
+            break
+    return first
+
+
 def label_medium(medium, max_labels: int = 256):
     """Exact label decomposition of the four property volumes, or None.
 
@@ -118,17 +133,23 @@ def label_medium(medium, max_labels: int = 256):
     most ``max_labels`` distinct (alpha, rho, c, beta) tuples.
     """
     vols = [np.ascontiguousarray(getattr(medium, k), np.float32) for k in ("alpha", "rho", "c", "beta")]
-    bits = [v.reshape(-1).view(np.uint32).astype(np.uint64) for v in vols]
     id_map = getattr(medium, "id_map", None)
     if id_map is not None:
-        ids, inv = np.unique(np.asarray(id_map).reshape(-1), return_inverse=True)
-        if len(ids) <= max_labels:
-            first = np.zeros(len(ids), np.int64)
-            first[inv[::-1]] = np.arange(len(inv))[::-1]
-            props = np.stack([v.reshape(-1)[first] for v in vols], axis=1)
-            ok = all(np.array_equal(props[inv, i], vols[i].reshape(-1)) for i in range(4))
-            if ok:
-                return inv.astype(np.uint8).reshape(vols[0].shape), props.astype(np.float32)
+        ids_flat = np.asarray(id_map).reshape(-1)
+        lo, hi = int(ids_flat.min()), int(ids_flat.max())
+        if hi - lo < (1 << 20):
+            # small integer range: O(N) relabel through a lookup table
+            present = np.flatnonzero(np.bincount(ids_flat - lo, minlength=hi - lo + 1))
+            if len(present) <= max_labels:
+                lut = np.zeros(hi - lo + 1, np.int64)
+                lut[present] = np.arange(len(present))
+                inv = lut[ids_flat - lo]
+                first = _first_occurrence(inv, len(present))
+                props = np.stack([v.reshape(-1)[first] for v in vols], axis=1)
+                ok = all(np.array_equal(props[inv, i], vols[i].reshape(-1)) for i in range(4))
+                if ok:
+                    return inv.astype(np.uint8).reshape(vols[0].shape), props.astype(np.float32)
+    bits = [v.reshape(-1).view(np.uint32).astype(np.uint64) for v in vols]
     for b in bits:
         if len(np.unique(b[:: max(1, b.size // 4096)])) > max_labels:
             return None
@@ -210,9 +231,9 @@ class Plan:
     def ncell(self) -> int:
         return int(np.prod(self.padded3))
 
-    def drive_table(self) -> np.ndarray:
+    def drive_table(self, n_steps: int | None = None) -> np.ndarray:
         """(amp ramp(t), sin wt, cos wt, 0) per step (engine.py:478-482, sources.py:98-102)."""
-        n_steps = self.max_periods * self.spp
+        n_steps = self.max_periods * self.spp if n_steps is None else int(n_steps)
         out = np.zeros((n_steps, 4), np.float32)
         for n in range(n_steps):
             t = n * self.dt
@@ -364,6 +385,11 @@ class DeviceSolver:
             raise ValueError(f"phases for {ac.shape[0]} members given to a batch of {self.batch}")
         xyz = np.ascontiguousarray(self.plan.src_xyz)
         _lib.call("cg_solver_set_source", self.h, int(xyz.shape[0]), _lib.ptr(xyz), _lib.ptr(ac), _lib.ptr(as_))
+
+    def extend_drive(self, n_steps: int) -> None:
+        """Drive table covering ``n_steps`` steps (the default covers one solve's schedule)."""
+        self.drive = self.plan.drive_table(n_steps)
+        _lib.call("cg_solver_set_drive", self.h, len(self.drive), _lib.ptr(self.drive))
 
     def close(self) -> None:
         if getattr(self, "h", None):

@@ -27,6 +27,9 @@ extern "C" {
 const char* cg_last_error(void);
 /* CG_ABI_VERSION of the loaded library. */
 int cg_version(void);
+/* Make `device` current for this host thread; handles created afterwards
+ * live on it (one process per GPU). */
+int cg_set_device(int device);
 
 /* ---------------------------------------------------- k-space CW solver */
 
