@@ -86,6 +86,7 @@ SIGNATURES = {
     "cg_fft3d_destroy": [_P],
     "cg_fft3d_forward": [_P, _P, _P],
     "cg_fft3d_inverse": [_P, _P, _P],
+    "cg_fft3d_forward_noalloc": [_I, _I, _I, _I, _P, _P, _P],
     "cg_pennes_create": [C.POINTER(PennesConfig), C.POINTER(_P)],
     "cg_pennes_destroy": [_P],
     "cg_pennes_set_coefficients": [_P, _P, _P, _P, _P, _P, _P, _P, _P],

@@ -1447,3 +1447,91 @@ extern "C" int cg_fft3d_inverse(cg_fft3d* f, const float* in_spec, float* out) {
   CG_CUDA_TRY(cudaStreamSynchronize(f->stream));
   return CG_OK;
 }
+
+// ------------------------------------- 3-D forward FFT without allocation --
+// For callers that may not allocate device memory themselves: code that runs
+// inside another framework's memory pool (every byte accounted for by that
+// pool), serving loops that must not pay cudaMalloc's implicit device-wide
+// synchronisation, and plug-ins whose host application owns the CUDA heap.
+// The transform's only scratch -- the three per-axis twiddle tables -- lives
+// in this fixed array, reserved on every device that loads the library until
+// the process exits. Inputs and outputs are the caller's device buffers.
+#define CG_NOALLOC_AXIS_MAX CG_MAX_N  // longest axis the array can hold tables for
+static __device__ __align__(256) float2 g_noalloc_twiddles[3 * CG_NOALLOC_AXIS_MAX];
+
+#include <mutex>
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[128];  // per-device address of g_noalloc_twiddles
+
+// Once per device, with that device current: resolve the array's device
+// address (the host-side symbol is only a stand-in) and lift the kernels'
+// dynamic shared-memory limit. Neither allocates.
+static int noalloc_setup(int dev, float2** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    CG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_twiddles));
+    CG_CUDA_TRY(allow_max_smem((const void*)k_ypass));
+    CG_CUDA_TRY(allow_max_smem((const void*)k_xpass));
+    CG_CUDA_TRY(allow_max_smem((const void*)k_zpass_p));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = (float2*)g_noalloc_ptr[dev];
+  return CG_OK;
+}
+
+extern "C" int cg_fft3d_forward_noalloc(int nx, int ny, int nz, int batch, const float* in_dev, float* out_dev,
+                                        void* stream) {
+  CG_REQUIRE(in_dev && out_dev, "null argument");
+  CG_REQUIRE(batch >= 1 && batch <= 65535, "batch %d out of range", batch);
+  CG_REQUIRE(nx >= 1 && ny >= 1 && nz >= 2, "invalid FFT shape %dx%dx%d", nx, ny, nz);
+  CG_REQUIRE(nx <= CG_NOALLOC_AXIS_MAX && ny <= CG_NOALLOC_AXIS_MAX && nz <= CG_NOALLOC_AXIS_MAX,
+             "FFT shape %dx%dx%d exceeds the fixed scratch of the no-allocation entry point (every axis <= %d)",
+             nx, ny, nz, CG_NOALLOC_AXIS_MAX);
+  Dims d;
+  d.nx = nx; d.ny = ny; d.nz = nz; d.nzh = nz / 2 + 1;
+  d.ncell = (long long)nx * ny * nz;
+  d.nspec = (long long)nx * d.nzh * ny;
+  AxisPlan px, py, pz;
+  if (cg_make_plan(nx, &px) || cg_make_plan(ny, &py) || cg_make_plan(nz, &pz)) {
+    cg_set_error("FFT shape %dx%dx%d: every axis must be 2/3/5-smooth", nx, ny, nz);
+    return CG_ERR_INVALID;
+  }
+  const size_t sy = smem_ypass(ny), sx = smem_xpass(nx), sz = smem_zpass(nz), lim = smem_limit();
+  CG_REQUIRE(sy <= lim && sx <= lim && sz <= lim,
+             "FFT shape %dx%dx%d needs more shared memory per tile than the device offers", nx, ny, nz);
+  int dev = 0;
+  CG_CUDA_TRY(cudaGetDevice(&dev));
+  CG_REQUIRE(dev >= 0 && dev < 128, "device ordinal %d out of range", dev);
+  float2* tw = nullptr;
+  int rc = noalloc_setup(dev, &tw);
+  if (rc != CG_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the tables are rewritten by every call: nothing carries over between calls
+  k_twiddles<<<(nx + 255) / 256, 256, 0, st>>>(tw, nx);
+  k_twiddles<<<(ny + 255) / 256, 256, 0, st>>>(tw + CG_NOALLOC_AXIS_MAX, ny);
+  k_twiddles<<<(nz + 255) / 256, 256, 0, st>>>(tw + 2 * CG_NOALLOC_AXIS_MAX, nz);
+  Tables t;
+  t.twx = tw;
+  t.twy = tw + CG_NOALLOC_AXIS_MAX;
+  t.twz = tw + 2 * CG_NOALLOC_AXIS_MAX;
+  // k and sponge tables are never read by the plain transform passes
+  t.kx = t.ky = t.kz = t.kx2 = t.ky2 = t.kz2 = t.sx = t.sy = t.sz = (const float*)tw;
+  MediumDev m;
+  memset(&m, 0, sizeof(m));
+  SourceDev sd;
+  memset(&sd, 0, sizeof(sd));
+  RecordDev rd;
+  memset(&rd, 0, sizeof(rd));
+  rd.spp = 1;
+  float2* spec = (float2*)out_dev;
+  const dim3 gy((unsigned)((d.nx * (long long)d.nzh + CG_TILE - 1) / CG_TILE), batch);
+  const dim3 gx((unsigned)(((long long)d.nzh * d.ny + CG_TILE - 1) / CG_TILE), batch);
+  const dim3 gz((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
+  k_zpass_p<<<gz, CG_THREADS, sz, st>>>(0, d, pz, t, m, sd, rd, nullptr, 0, 0, (float*)in_dev, spec);
+  k_ypass<<<gy, CG_THREADS, sy, st>>>(Y_FWD, d, py, t, spec, nullptr, nullptr);
+  k_xpass<<<gx, CG_THREADS, sx, st>>>(X_FWD, d, px, t, 0.f, 1.f, spec, nullptr, nullptr);
+  CG_CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}

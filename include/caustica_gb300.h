@@ -123,6 +123,24 @@ int cg_fft3d_destroy(cg_fft3d* f);
 int cg_fft3d_forward(cg_fft3d* f, const float* in, float* out_spec);
 int cg_fft3d_inverse(cg_fft3d* f, const float* in_spec, float* out);
 
+/* The forward transform above for callers that may not allocate device
+ * memory: code running inside another framework's memory pool, serving
+ * loops that must avoid cudaMalloc's implicit synchronisation, plug-ins
+ * whose host application owns the CUDA heap. No counterpart in the
+ * reference (it has no device code). in_dev [batch][x][y][z] float32 and
+ * out_dev [batch][x][kz][y] complex64 are the caller's device buffers;
+ * work is queued on `stream` (a cudaStream_t, NULL = legacy default) and
+ * the call returns without synchronising. The only scratch, three per-axis
+ * twiddle tables, lives in a fixed 48 KB device array that every GPU which
+ * loads the library keeps until the process exits; every axis must be
+ * <= 2048 (larger shapes are refused with CG_ERR_INVALID). The first call on
+ * a device resolves that array's address there, so make it before any
+ * stream capture. Calls share the array and rewrite it in full: calls whose
+ * work overlaps on the GPU (different streams, no ordering) race. No
+ * cudaMalloc, cudaFree or allocating library call is made. */
+int cg_fft3d_forward_noalloc(int nx, int ny, int nz, int batch, const float* in_dev, float* out_dev,
+                             void* stream);
+
 /* -------------------------------------------------------- Pennes / CEM43 */
 
 typedef struct cg_pennes cg_pennes;
