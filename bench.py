@@ -319,12 +319,94 @@ def run_gb300(args, dist, rank, ws, local):
                        "step": f"one full solve ({res.steps_total} time steps, {res.steps_total // plan.spp} periods) "
                                f"through WesterveltKSpaceGB300.run() from host numpy",
                        "seconds": el, "solves_per_s": ws / el}
+    if rank == 0 and ws == 1 and not args.skip_batched:
+        line["batched"] = bench_batched()
+    if rank == 0 and ws == 1 and not args.skip_serving:
+        line["serving"] = bench_serving()
     if rank == 0 and ws == 1 and not args.skip_cpu:
         cb = cpu_sample(job, target_s=float(os.environ.get("CG_CPU_SECONDS", "12")))
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line["clocks"] = clk.summary()
     if rank == 0:
         print(json.dumps(line, default=_jsonable), flush=True)
+
+
+def bench_batched(n_plain: int = 4):
+    """Config 4: 64 steering positions over one medium, plain (one solve per
+    call) against batched (all members in one handle), both end to end
+    through the public API from host numpy."""
+    import time as _t
+
+    from caustica_gb300 import workloads as wl
+    from caustica_gb300.batch import solve_steering
+    from caustica_gb300.contract import CWSource
+    from caustica_gb300.solvers import LinearKSpaceGB300
+
+    job = wl.config4(64)
+    grid, med, spec = job["grid"], job["medium"], job["spec"]
+    idx, phases = job["source"].indices, job["phases"]
+    solver = LinearKSpaceGB300()
+
+    def plain(b):
+        src = CWSource(indices=idx, phases=phases[b], amplitude=1e5, f0=1e6)
+        return solver.run(grid, med, src, spec, reference_point=job["reference_point"])
+
+    plain(0)  # warm
+    t0 = _t.perf_counter()
+    for b in range(n_plain):
+        r = plain(b)
+    t_plain = (_t.perf_counter() - t0) / n_plain
+    t0 = _t.perf_counter()
+    res = solve_steering(grid, med, idx, phases, f0=1e6, amplitude=1e5, spec=spec,
+                         reference_point=job["reference_point"])
+    t_batch = _t.perf_counter() - t0
+    cells = int(np.prod(grid.shape))
+    cell_steps = cells * r.steps_total
+    return {"workload": job["name"], "members": len(res), "steps_per_solve": r.steps_total,
+            "plain_solves_per_s": 1.0 / t_plain, "batched_solves_per_s": len(res) / t_batch,
+            "ratio": (len(res) / t_batch) * t_plain, "batched_cell_steps_per_s": len(res) * cell_steps / t_batch,
+            "plain_cell_steps_per_s": cell_steps / t_plain, "plain_sample": f"{n_plain} solves",
+            "timing": "wall clock of the public calls (host numpy in, host numpy out)"}
+
+
+def bench_serving(n_req: int = 16, seed: int = 5):
+    """Config 5: a served request stream; capacity with all requests queued at
+    once, then Poisson arrivals at 0.5x and 0.9x that capacity."""
+    import time as _t
+
+    from caustica_gb300 import serve
+    from caustica_gb300 import workloads as wl
+
+    reqs = wl.config5_requests(n_req, seed)
+
+    def run(rate):
+        rng = np.random.default_rng(seed + 1)
+        arr = np.zeros(len(reqs)) if rate is None else np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+        with serve.Server(hbm_budget_bytes=160 << 30) as srv:
+            t0 = _t.perf_counter()
+            futs = []
+            for r, ta in zip(reqs, arr):
+                dt = t0 + ta - _t.perf_counter()
+                if dt > 0:
+                    _t.sleep(dt)
+                futs.append(srv.submit(r))
+            outs = [f.result() for f in futs]
+            wall = _t.perf_counter() - t0
+            stats = dict(srv.stats)
+        lat = np.array([o.latency_s for o in outs])
+        return {"offered_rate": rate, "solves_per_s": len(outs) / wall, "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99)), "wall_s": wall, "groups": stats["groups"],
+                "max_active": stats["max_active"], "peak_gb": stats["peak_bytes"] / 1e9}
+
+    run(None)  # warm (plans, allocations)
+    cap = run(None)
+    points = [cap] + [run(f * cap["solves_per_s"]) for f in (0.5, 0.9)]
+    shapes = {}
+    for r in reqs:
+        shapes[str(r.tag["shape"])] = shapes.get(str(r.tag["shape"]), 0) + 1
+    return {"requests": len(reqs), "grids": shapes, "thermal": sum(r.tag["thermal"] for r in reqs),
+            "westervelt": sum(r.tag["nonlinear"] for r in reqs), "capacity_solves_per_s": cap["solves_per_s"],
+            "points": points, "note": f"p99 over {len(reqs)} requests per point"}
 
 
 class C_float:
@@ -351,6 +433,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--prerun-periods", type=int, default=None,
                     help="periods run before the warm-up (default: the settle floor of the workload)")
     args = ap.parse_args()

@@ -79,6 +79,7 @@ SIGNATURES = {
     "cg_solver_get_state": [_P, _P, _P],
     "cg_solver_set_state": [_P, _P, _P, _LL],
     "cg_solver_synchronize": [_P],
+    "cg_solver_query": [_P, _P],
     "cg_solver_info": [_P, _P],
     "cg_solver_timed_run": [_P, _I, _I, _I, _P],
     "cg_solver_profile": [_P, _I, _I, _P],

@@ -23,7 +23,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libcaustica_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["cg_kspace.cu", "cg_pennes.cu"]
+SOURCES = ["cg_kspace.cu", "cg_pennes.cu", "cg_fast_yx.cu", "cg_fast_z.cu"]
 
 
 def nvcc() -> str:
@@ -38,6 +38,9 @@ def _flags(verbose_ptxas: bool = False) -> list[str]:
          f"-I{INCLUDE}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
     if verbose_ptxas:
         f.append("-Xptxas=-v")
+    for var in ("CG_FAST_MINB_YX", "CG_FAST_MINB_Z"):
+        if os.environ.get(var):
+            f.append(f"-D{var}={int(os.environ[var])}")
     return f
 
 

@@ -1,0 +1,225 @@
+// Size-specialised y- and x-passes (axis length N known at compile time).
+//
+// y-pass: rows (x, kz) of length ny, 16 rows per CTA; thread (p, s) =
+// (threadIdx / 16, threadIdx % 16) owns row p. x-pass: 16 consecutive
+// (kz, y) columns per CTA; thread (c, s) = (threadIdx % 16, threadIdx / 16)
+// owns column c. Pencil data moves global -> registers -> one exchange per
+// transform -> registers -> global (cg_fast.cuh).
+#include "cg_fast.cuh"
+#include "cg_kspace.cuh"
+
+// resident CTAs per SM the register allocation targets
+#ifndef CG_FAST_MINB_YX
+#define CG_FAST_MINB_YX 3
+#endif
+#define CG_FAST_MINB CG_FAST_MINB_YX
+
+using cgf::ColEx;
+using cgf::RowEx;
+using cgf::Split;
+using cgf::fft2;
+using cgf::static_for;
+
+template <int N>
+__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_ypass(int mode, Dims d, Tables t, float2* __restrict__ S0,
+                                                         float2* __restrict__ S1, float2* __restrict__ S2) {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  using Ex = RowEx<A, B>;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;  // (A, B) order
+  cgf::fill_twt<A, B>(tw, t.twy);
+  const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
+  const Ex ex{sm + N + p * Ex::SLAB};
+  const long long nrows = (long long)d.nx * d.nzh;
+  const long long row = (long long)blockIdx.x * CG_TILE + p;
+  const bool valid = row < nrows;
+  const long long off = (long long)blockIdx.y * d.nspec + row * N;
+  __syncthreads();
+  float2 v[A], w[B];
+  auto load = [&](const float2* __restrict__ src) {
+    static_for<0, A>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      v[a] = (valid && s < B) ? src[off + s + B * a] : make_float2(0.f, 0.f);
+    });
+  };
+  auto store = [&](float2* __restrict__ dst) {
+    if (valid && s < A) static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      dst[off + s + A * b] = w[b];
+    });
+  };
+  if (mode == Y_FWD || mode == Y_INV) {
+    load(S0);
+    if (mode == Y_FWD) fft2<A, B, false>(v, w, s, tw, ex);
+    else fft2<A, B, true>(v, w, s, tw, ex);
+    store(S0);
+    return;
+  }
+  if (mode == Y_INV_GRAD) {
+    load(S1);
+    fft2<A, B, true>(v, w, s, tw, ex);
+    store(S1);
+    load(S2);
+    float2 g[A];
+    static_for<0, A>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      const float k = (s < B) ? t.ky[s + B * a] : 0.f;
+      g[a] = c_muli(c_scale(v[a], k));
+    });
+    fft2<A, B, true>(g, w, s, tw, ex);
+    store(S0);
+    fft2<A, B, true>(v, w, s, tw, ex);
+    store(S2);
+    return;
+  }
+  // Y_FWD_DIV: S1 = FFT(S1); S0 = i ky FFT(S0) + FFT(S2)
+  load(S1);
+  fft2<A, B, false>(v, w, s, tw, ex);
+  store(S1);
+  load(S0);
+  fft2<A, B, false>(v, w, s, tw, ex);
+  float2 h[B];
+  static_for<0, B>([&](auto bi) {
+    constexpr int b = decltype(bi)::value;
+    const float k = (s < A) ? t.ky[s + A * b] : 0.f;
+    h[b] = c_muli(c_scale(w[b], k));
+  });
+  load(S2);
+  fft2<A, B, false>(v, w, s, tw, ex);
+  static_for<0, B>([&](auto bi) { w[decltype(bi)::value] = c_add(w[decltype(bi)::value], h[decltype(bi)::value]); });
+  store(S0);
+}
+
+template <int N>
+__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_xpass(int mode, Dims d, Tables t, float kcoef, float invN,
+                                                         float2* __restrict__ S0, float2* __restrict__ S1,
+                                                         float2* __restrict__ S2) {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;       // (A, B) order
+  float2* twi = sm + N;  // (B, A) order
+  cgf::fill_twt<A, B>(tw, t.twx);
+  cgf::fill_twt<B, A>(twi, t.twx);
+  const int c = threadIdx.x & 15, s = threadIdx.x >> 4;
+  const ColEx<A, B> exf{sm + 2 * N + c};
+  const ColEx<B, A> exi{sm + 2 * N + c};
+  const long long ncol = (long long)d.nzh * d.ny;
+  const long long col = (long long)blockIdx.x * CG_TILE + c;
+  const bool valid = col < ncol;
+  const long long base = (long long)blockIdx.y * d.nspec + col;
+  float kyz2 = 0.f;
+  {
+    const long long cc = valid ? col : ncol - 1;
+    const int kz = (int)(cc / d.ny);
+    const int ky = (int)(cc - (long long)kz * d.ny);
+    kyz2 = t.ky2[ky] + t.kz2[kz];
+  }
+  __syncthreads();
+  float2 v[A], w[B], z[A];
+  auto load = [&](const float2* __restrict__ src) {
+    static_for<0, A>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      v[a] = (valid && s < B) ? src[base + (long long)(s + B * a) * ncol] : make_float2(0.f, 0.f);
+    });
+  };
+  // after an inverse (B, A) transform thread s < B owns z[a] = element s + B a
+  auto store_z = [&](float2* __restrict__ dst) {
+    if (valid && s < B) static_for<0, A>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      dst[base + (long long)(s + B * a) * ncol] = z[a];
+    });
+  };
+  auto kappa = [&](int k) { return sinc_a2(kcoef * (t.kx2[k] + kyz2)) * invN; };
+  if (mode == X_FWD || mode == X_INV) {
+    load(S0);
+    if (mode == X_FWD) fft2<A, B, false>(v, w, s, tw, exf);
+    else fft2<A, B, true>(v, w, s, tw, exf);
+    if (valid && s < A) static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      S0[base + (long long)(s + A * b) * ncol] = w[b];
+    });
+    return;
+  }
+  if (mode == X_GRAD) {
+    load(S0);
+    fft2<A, B, false>(v, w, s, tw, exf);
+    float2 g[B];
+    static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const int k = (s < A) ? s + A * b : 0;
+      const float2 q = c_scale(w[b], kappa(k));
+      w[b] = q;
+      g[b] = c_muli(c_scale(q, t.kx[k]));
+    });
+    fft2<B, A, true>(w, z, s, twi, exi);
+    store_z(S2);
+    fft2<B, A, true>(g, z, s, twi, exi);
+    store_z(S1);
+    return;
+  }
+  // X_DIV: S0 = IFFT(kappa/N (FFT(S0) + i kx FFT(S1)))
+  load(S1);
+  fft2<A, B, false>(v, w, s, tw, exf);
+  float2 h[B];
+  static_for<0, B>([&](auto bi) { h[decltype(bi)::value] = w[decltype(bi)::value]; });
+  load(S0);
+  fft2<A, B, false>(v, w, s, tw, exf);
+  static_for<0, B>([&](auto bi) {
+    constexpr int b = decltype(bi)::value;
+    const int k = (s < A) ? s + A * b : 0;
+    w[b] = c_scale(c_add(w[b], c_muli(c_scale(h[b], t.kx[k]))), kappa(k));
+  });
+  fft2<B, A, true>(w, z, s, twi, exi);
+  store_z(S0);
+}
+
+template <int N>
+static size_t smem_y() {
+  return sizeof(float2) * (N + CG_TILE * RowEx<Split<N>::A, Split<N>::B>::SLAB);
+}
+template <int N>
+static size_t smem_x() {
+  return sizeof(float2) * (2 * N + (size_t)N * CG_TILE);
+}
+
+bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1, float2* S2, int batch,
+                cudaStream_t st) {
+  const dim3 grid((unsigned)((d.nx * (long long)d.nzh + CG_TILE - 1) / CG_TILE), batch);
+  switch (d.ny) {
+#define CASE(n)                                                                   \
+  case n:                                                                         \
+    kf_ypass<n><<<grid, CG_THREADS, smem_y<n>(), st>>>(mode, d, t, S0, S1, S2); \
+    return true;
+    CG_FAST_SIZES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float invN, float2* S0, float2* S1,
+                float2* S2, int batch, cudaStream_t st) {
+  const dim3 grid((unsigned)(((long long)d.nzh * d.ny + CG_TILE - 1) / CG_TILE), batch);
+  switch (d.nx) {
+#define CASE(n)                                                                                    \
+  case n:                                                                                          \
+    kf_xpass<n><<<grid, CG_THREADS, smem_x<n>(), st>>>(mode, d, t, kcoef, invN, S0, S1, S2); \
+    return true;
+    CG_FAST_SIZES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+int fast_prepare_yx() {
+#define SET(n)                                                                                      \
+  if (cudaFuncSetAttribute(kf_ypass<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<n>()) != \
+          cudaSuccess ||                                                                            \
+      cudaFuncSetAttribute(kf_xpass<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<n>()) != \
+          cudaSuccess)                                                                              \
+    return -1;
+  CG_FAST_SIZES(SET)
+#undef SET
+  return 0;
+}

@@ -50,98 +50,7 @@ extern "C" int cg_set_device(int device) {
   return CG_OK;
 }
 
-// ------------------------------------------------------------ structures --
-#define CG_TILE 16   // pencils per tile
-#define CG_ZROWS 32  // real rows per z tile (two per complex pencil)
-#define CG_MAX_H 8
-#define CG_THREADS 256
-
-struct Dims {
-  int nx, ny, nz, nzh;
-  long long ncell;  // nx*ny*nz
-  long long nspec;  // nx*nzh*ny
-};
-
-struct Tables {
-  const float2* twx;
-  const float2* twy;
-  const float2* twz;
-  const float* kx;  // derivative wavenumbers, Nyquist zeroed
-  const float* ky;
-  const float* kz;
-  const float* kx2;  // true k^2
-  const float* ky2;
-  const float* kz2;
-  const float* sx;  // sponge profiles
-  const float* sy;
-  const float* sz;
-};
-
-struct MediumDev {
-  const uint8_t* labels;  // null when dense
-  const float4* ltab;     // per label (dt/rho, rho c^2 dt, absorb, 2 beta dt)
-  const float* dtr;
-  const float* rc2;
-  const float* ab;
-  const float* b2;  // null when linear
-  int nonlinear;
-};
-
-struct SourceDev {
-  const int* row_ptr;  // CSR over rows x*ny + y (size nx*ny + 1)
-  const int* zidx;     // z of each source voxel
-  const float* ac;     // [B][S] scale * cos(phase)
-  const float* as;     // [B][S] scale * sin(phase)
-  int S;
-  const float4* drive;  // per step: (amp*env, sin wt, cos wt, 0)
-  int n_drive;
-};
-
-struct RecordDev {
-  int lo[3], hi[3];  // record box (padded coords, inside the active grid)
-  long long nrec;
-  float* bins;  // [B][spp][nrec]
-  float* comp;  // [B][spp][nrec]  Kahan compensation
-  float* pmax;  // [B][nrec]
-  int clo[3], chi[3];  // convergence box
-  unsigned int* peaks;  // [B][max_periods] float bits of the per-period max |p|
-  int max_periods;
-  int spp;
-};
-
-// -------------------------------------------------------------- helpers --
-__device__ __forceinline__ float sinc_a2(float a2) {
-  // sin(a)/a = sum_n (-1)^n a^(2n) / (2n+1)!, truncated after a^14; for
-  // a <= 2 the first omitted term is below 2e-10.
-  if (a2 > 4.0f) {
-    float a = sqrtf(a2);
-    return sinf(a) / a;
-  }
-  float r = -7.6471637318198164759e-13f;
-  r = fmaf(r, a2, 1.6059043836821614599e-10f);
-  r = fmaf(r, a2, -2.5052108385441718775e-08f);
-  r = fmaf(r, a2, 2.7557319223985890653e-06f);
-  r = fmaf(r, a2, -1.9841269841269841270e-04f);
-  r = fmaf(r, a2, 8.3333333333333333333e-03f);
-  r = fmaf(r, a2, -1.6666666666666666667e-01f);
-  r = fmaf(r, a2, 1.0f);
-  return r;
-}
-
-__device__ __forceinline__ void load_tw(float2* dst, const float2* src, int n) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
-}
-
-// coefficients of one cell: (dt/rho, rho c^2 dt, absorb, 2 beta dt)
-__device__ __forceinline__ float4 cell_coef(const MediumDev& m, long long i) {
-  if (m.labels) return m.ltab[m.labels[i]];
-  float4 r;
-  r.x = m.dtr[i];
-  r.y = m.rc2[i];
-  r.z = m.ab[i];
-  r.w = m.b2 ? m.b2[i] : 0.0f;
-  return r;
-}
+#include "cg_kspace.cuh"
 
 // ============================================================ y-pass ====
 // Rows (x, kz) of length ny, contiguous. A tile holds 16 rows as pencils:
@@ -170,7 +79,6 @@ __device__ __forceinline__ void y_store(float2* __restrict__ dst, const float2* 
   }
 }
 
-enum YMode { Y_FWD = 0, Y_INV = 1, Y_INV_GRAD = 2, Y_FWD_DIV = 3 };
 
 // S0 forward/inverse in place; GRAD: S1 -> inv -> S1, i ky S2 -> inv -> S0,
 // S2 -> inv -> S2; DIV: S1 -> fwd -> S1, i ky fwd(S0) + fwd(S2) -> S0.
@@ -260,7 +168,6 @@ __device__ __forceinline__ void x_store(float2* __restrict__ dst, const float2* 
   }
 }
 
-enum XMode { X_GRAD = 0, X_DIV = 1, X_FWD = 2, X_INV = 3 };
 
 // GRAD: S0 -> Q = kappa/N FFTx(S0); S1 = IFFTx(i kx Q), S2 = IFFTx(Q)
 // DIV : S0 = IFFTx(kappa/N (FFTx(S0) + i kx FFTx(S1)))
@@ -935,6 +842,7 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_xpass);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_zpass_u);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_zpass_p);
+  if (e == cudaSuccess && fast_prepare() != 0) e = cudaErrorInvalidValue;
   if (e != cudaSuccess) {
     cg_set_error("solver set-up: %s", cudaGetErrorString(e));
     solver_free(s);
@@ -1113,22 +1021,30 @@ static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = 
 #define EV(i) \
   if (ev) cudaEventRecord(ev[i], st)
   EV(0);
-  k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD, d, s->py, t, s->S0, s->S1, s->S2);
+  if (!fast_ypass(Y_FWD, d, t, s->S0, s->S1, s->S2, B, st))
+    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD, d, s->py, t, s->S0, s->S1, s->S2);
   EV(1);
-  k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_GRAD, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
+  if (!fast_xpass(X_GRAD, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
+    k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_GRAD, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
   EV(2);
-  k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
+  if (!fast_ypass(Y_INV_GRAD, d, t, s->S0, s->S1, s->S2, B, st))
+    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
   EV(3);
-  k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
+  if (!fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st))
+    k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
   EV(4);
-  k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD_DIV, d, s->py, t, s->S0, s->S1, s->S2);
+  if (!fast_ypass(Y_FWD_DIV, d, t, s->S0, s->S1, s->S2, B, st))
+    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD_DIV, d, s->py, t, s->S0, s->S1, s->S2);
   EV(5);
-  k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_DIV, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
+  if (!fast_xpass(X_DIV, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
+    k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_DIV, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
   EV(6);
-  k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
+  if (!fast_ypass(Y_INV, d, t, s->S0, s->S1, s->S2, B, st))
+    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
   EV(7);
-  k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
-                                               record, s->p, s->S0);
+  if (!fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st))
+    k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
+                                                 record, s->p, s->S0);
   EV(8);
 #undef EV
   return CG_OK;
@@ -1238,8 +1154,10 @@ extern "C" int cg_solver_set_state(cg_solver* s, const float* p, const float* u,
   CG_CUDA_TRY(cudaMemcpyAsync(s->u, u, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
   k_set_ctl<<<1, 1, 0, s->stream>>>(s->ctl, step);
   const dim3 gz((unsigned)(s->d.nx * ((s->d.ny + CG_ZROWS - 1) / CG_ZROWS)), s->B);
-  k_zpass_p<<<gz, CG_THREADS, s->smem_z, s->stream>>>(0, s->d, s->pz, make_tables(s), make_medium(s),
-                                                       make_source(s), make_record(s), s->ctl, 0, 0, s->p, s->S0);
+  if (!fast_zpass_p(0, s->d, make_tables(s), make_medium(s), make_source(s), make_record(s), s->ctl, 0, 0, s->p,
+                    s->S0, s->B, s->stream))
+    k_zpass_p<<<gz, CG_THREADS, s->smem_z, s->stream>>>(0, s->d, s->pz, make_tables(s), make_medium(s),
+                                                         make_source(s), make_record(s), s->ctl, 0, 0, s->p, s->S0);
   CG_CUDA_TRY(cudaGetLastError());
   CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   return CG_OK;
@@ -1249,6 +1167,18 @@ extern "C" int cg_solver_synchronize(cg_solver* s) {
   CG_REQUIRE(s, "null solver");
   CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   CG_CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+extern "C" int cg_solver_query(cg_solver* s, int* idle) {
+  CG_REQUIRE(s && idle, "null argument");
+  cudaError_t e = cudaStreamQuery(s->stream);
+  if (e == cudaErrorNotReady) {
+    *idle = 0;
+    return CG_OK;
+  }
+  CG_CUDA_TRY(e);
+  *idle = 1;
   return CG_OK;
 }
 
@@ -1370,6 +1300,7 @@ extern "C" int cg_fft3d_create(int nx, int ny, int nz, int batch, cg_fft3d** out
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_ypass);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_xpass);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_zpass_p);
+  if (e == cudaSuccess && fast_prepare() != 0) e = cudaErrorInvalidValue;
   if (e == cudaSuccess && (f->smem_y > smem_limit() || f->smem_x > smem_limit() || f->smem_z > smem_limit())) {
     cg_set_error("FFT shape %dx%dx%d needs more shared memory per tile than the device offers", nx, ny, nz);
     fft_free(f);
@@ -1415,9 +1346,12 @@ extern "C" int cg_fft3d_forward(cg_fft3d* f, const float* in, float* out_spec) {
   const dim3 gy((unsigned)((d.nx * (long long)d.nzh + CG_TILE - 1) / CG_TILE), f->B);
   const dim3 gx((unsigned)(((long long)d.nzh * d.ny + CG_TILE - 1) / CG_TILE), f->B);
   const dim3 gz((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), f->B);
-  k_zpass_p<<<gz, CG_THREADS, f->smem_z, f->stream>>>(0, d, f->pz, t, m, sd, rd, nullptr, 0, 0, f->real, f->spec);
-  k_ypass<<<gy, CG_THREADS, f->smem_y, f->stream>>>(Y_FWD, d, f->py, t, f->spec, nullptr, nullptr);
-  k_xpass<<<gx, CG_THREADS, f->smem_x, f->stream>>>(X_FWD, d, f->px, t, 0.f, 1.f, f->spec, nullptr, nullptr);
+  if (!fast_zpass_p(0, d, t, m, sd, rd, nullptr, 0, 0, f->real, f->spec, f->B, f->stream))
+    k_zpass_p<<<gz, CG_THREADS, f->smem_z, f->stream>>>(0, d, f->pz, t, m, sd, rd, nullptr, 0, 0, f->real, f->spec);
+  if (!fast_ypass(Y_FWD, d, t, f->spec, nullptr, nullptr, f->B, f->stream))
+    k_ypass<<<gy, CG_THREADS, f->smem_y, f->stream>>>(Y_FWD, d, f->py, t, f->spec, nullptr, nullptr);
+  if (!fast_xpass(X_FWD, d, t, 0.f, 1.f, f->spec, nullptr, nullptr, f->B, f->stream))
+    k_xpass<<<gx, CG_THREADS, f->smem_x, f->stream>>>(X_FWD, d, f->px, t, 0.f, 1.f, f->spec, nullptr, nullptr);
   CG_CUDA_TRY(cudaGetLastError());
   CG_CUDA_TRY(cudaMemcpyAsync(out_spec, f->spec, sizeof(float2) * f->B * d.nspec, cudaMemcpyDefault, f->stream));
   CG_CUDA_TRY(cudaStreamSynchronize(f->stream));
@@ -1439,9 +1373,12 @@ extern "C" int cg_fft3d_inverse(cg_fft3d* f, const float* in_spec, float* out) {
   const dim3 gy((unsigned)((d.nx * (long long)d.nzh + CG_TILE - 1) / CG_TILE), f->B);
   const dim3 gx((unsigned)(((long long)d.nzh * d.ny + CG_TILE - 1) / CG_TILE), f->B);
   const dim3 gz((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), f->B);
-  k_xpass<<<gx, CG_THREADS, f->smem_x, f->stream>>>(X_INV, d, f->px, t, 0.f, 1.f, f->spec, nullptr, nullptr);
-  k_ypass<<<gy, CG_THREADS, f->smem_y, f->stream>>>(Y_INV, d, f->py, t, f->spec, nullptr, nullptr);
-  k_zpass_p<<<gz, CG_THREADS, f->smem_z, f->stream>>>(2, d, f->pz, t, m, sd, rd, nullptr, 0, 0, f->real, f->spec);
+  if (!fast_xpass(X_INV, d, t, 0.f, 1.f, f->spec, nullptr, nullptr, f->B, f->stream))
+    k_xpass<<<gx, CG_THREADS, f->smem_x, f->stream>>>(X_INV, d, f->px, t, 0.f, 1.f, f->spec, nullptr, nullptr);
+  if (!fast_ypass(Y_INV, d, t, f->spec, nullptr, nullptr, f->B, f->stream))
+    k_ypass<<<gy, CG_THREADS, f->smem_y, f->stream>>>(Y_INV, d, f->py, t, f->spec, nullptr, nullptr);
+  if (!fast_zpass_p(2, d, t, m, sd, rd, nullptr, 0, 0, f->real, f->spec, f->B, f->stream))
+    k_zpass_p<<<gz, CG_THREADS, f->smem_z, f->stream>>>(2, d, f->pz, t, m, sd, rd, nullptr, 0, 0, f->real, f->spec);
   CG_CUDA_TRY(cudaGetLastError());
   CG_CUDA_TRY(cudaMemcpyAsync(out, f->real, sizeof(float) * f->B * d.ncell, cudaMemcpyDefault, f->stream));
   CG_CUDA_TRY(cudaStreamSynchronize(f->stream));

@@ -331,6 +331,19 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
     )
 
 
+def device_footprint(plan: "Plan", batch: int) -> int:
+    """Device bytes of one solver handle (the serving loop's admission
+    estimate; the record accumulators are counted although they are only
+    allocated at the record window)."""
+    nx, ny, nz = plan.padded3
+    ncell = nx * ny * nz
+    nspec = nx * (nz // 2 + 1) * ny
+    nrec = int(np.prod([h - l for l, h in zip(plan.rec_lo, plan.rec_hi)]))
+    per_member = 16 * ncell + 24 * nspec + 8 * plan.spp * nrec + 4 * nrec + 8 * len(plan.harmonics) * nrec
+    medium = ncell if plan.labels is not None else 16 * ncell
+    return batch * per_member + medium + 16 * plan.max_periods * plan.spp + (64 << 10)
+
+
 # ----------------------------------------------------------------- device --
 class DeviceSolver:
     """One ``cg_solver`` handle: B right-hand sides over one medium."""
@@ -441,6 +454,16 @@ class DeviceSolver:
 
     def synchronize(self):
         _lib.call("cg_solver_synchronize", self.h)
+
+    def idle(self) -> bool:
+        """True when all queued work on this solver's stream has finished (non-blocking)."""
+        flag = C.c_int(0)
+        _lib.call("cg_solver_query", self.h, C.byref(flag))
+        return bool(flag.value)
+
+    def footprint_bytes(self) -> int:
+        """Device bytes this handle holds (state, spectra, medium, record buffers)."""
+        return device_footprint(self.plan, self.batch)
 
     def get_state(self):
         n = self.plan.ncell
@@ -560,14 +583,37 @@ def _results(plan: Plan, dev: DeviceSolver, ph, pm, common: dict, member: int, r
                       **common)
 
 
+def member_schedule(peaks: np.ndarray, plan: Plan, name: str | None = None):
+    """The settle decisions one member would take alone from its per-period
+    peaks (engine.py:484-510): (periods run, converged, converged_period,
+    history). Raises on the first non-finite peak."""
+    spec = plan.spec
+    prev = None
+    hist = []
+    for j, peak in enumerate(peaks, start=1):
+        peak = float(peak)
+        _guard_finite(peak, f"settling period {j} (step {j * plan.spp})", name or plan.name)
+        rel = abs(peak - prev) / max(prev, 1e-9) if prev is not None else None
+        if j >= plan.tof:
+            hist.append((j, peak, float("nan") if rel is None else rel))
+        if j >= plan.eff_min and rel is not None and peak > 0.0 and rel < spec.convergence_tol:
+            return j, True, j, hist
+        prev = peak
+        if j >= plan.eff_max:
+            break
+    return len(peaks), False, plan.eff_max, hist
+
+
 def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result_cls=SolverResult,
           dev: DeviceSolver | None = None):
     """Run the settle + record schedule; one result per batch member.
 
     With ``phases`` of shape (B, S) the B members share the medium and the
-    voxel set and differ in their drive phases (steering); the schedule is
-    decided by member 0 and shared, which is exact for a fixed schedule
-    (convergence_tol == 0) and for members whose peaks converge together.
+    voxel set and differ in their drive phases (steering). They run one
+    shared schedule, decided by member 0; every other member's own decisions
+    are replayed from its period peaks, and a member whose stand-alone run
+    would have stopped settling at a different period is solved again on
+    its own, so each result equals the one its solo run gives.
     """
     t0 = time.monotonic()
     batch = 1 if phases is None else int(np.atleast_2d(phases).shape[0])
@@ -580,7 +626,8 @@ def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result
             dev.set_phases(phases)
     try:
         spec = plan.spec
-        periods_done, converged, converged_period, history, _ = _settle(dev, plan, progress, 0, t0)
+        periods_done, converged, converged_period, history, all_peaks = _settle(dev, plan, progress, 0, t0)
+        settle_periods = periods_done
         if spec.t_end_min_us is not None:
             need = ceil(spec.t_end_min_us * 1e-6 / plan.period) - spec.n_record_periods
             if periods_done < need:
@@ -593,17 +640,32 @@ def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result
         dev.run_periods(spec.n_record_periods, record=True)
         ph, pm = dev.finalize(rec_steps)
         n = (periods_done + spec.n_record_periods) * plan.spp
+        peaks = np.array(all_peaks).T if all_peaks else np.zeros((batch, 0), np.float32)  # (B, periods)
+        results = []
+        redo = []
         for b in range(batch):
+            if b == 0:
+                sched = (settle_periods, converged, converged_period, history)
+            else:
+                sched = member_schedule(peaks[b], plan)
+                if sched[0] != settle_periods or sched[1] != converged:
+                    redo.append(b)
+                    results.append(None)
+                    continue
             _guard_finite(float(pm[b].max()), f"the record window (step {n})", plan.name)
-        common = dict(dt=plan.dt, spp=plan.spp, steps_total=n, t_end_s=n * plan.dt, tof_periods=plan.tof,
-                      converged_period=converged_period, settle_capped=not converged,
-                      convergence_history=history,
-                      meta={"solver": plan.name, "backend": "gb300", "padded_shape": plan.padded,
-                            "c_ref": plan.c_max, "nonlinear_active": plan.nonlinear_active,
-                            "source": plan.label,
-                            "medium_storage": "labels" if plan.labels is not None else "dense",
-                            "batch": batch})
-        return [_results(plan, dev, ph, pm, common, b, result_cls) for b in range(batch)]
+            common = dict(dt=plan.dt, spp=plan.spp, steps_total=n, t_end_s=n * plan.dt, tof_periods=plan.tof,
+                          converged_period=sched[2], settle_capped=not sched[1], convergence_history=sched[3],
+                          meta={"solver": plan.name, "backend": "gb300", "padded_shape": plan.padded,
+                                "c_ref": plan.c_max, "nonlinear_active": plan.nonlinear_active,
+                                "source": plan.label,
+                                "medium_storage": "labels" if plan.labels is not None else "dense",
+                                "batch": batch, "member": b})
+            results.append(_results(plan, dev, ph, pm, common, b, result_cls))
     finally:
         if own:
             dev.close()
+    for b in redo:
+        solo = solve(plan, phases=np.atleast_2d(phases)[b:b + 1], result_cls=result_cls)[0]
+        solo.meta.update({"batch": batch, "member": b, "solved_alone": True})
+        results[b] = solo
+    return results

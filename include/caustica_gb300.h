@@ -101,6 +101,9 @@ int cg_solver_finalize(cg_solver* s, int n_record_steps, float* phasors, float* 
 int cg_solver_get_state(cg_solver* s, float* p, float* u);
 int cg_solver_set_state(cg_solver* s, const float* p, const float* u, long long step);
 int cg_solver_synchronize(cg_solver* s);
+/* *idle = 1 when every call queued on the solver's stream has finished;
+ * never blocks (lets one host thread drive many solvers). */
+int cg_solver_query(cg_solver* s, int* idle);
 /* Device time [ms] of n_steps steps, CUDA events on the solver's stream;
  * graph != 0 runs whole periods through the captured graph. Synchronises. */
 int cg_solver_timed_run(cg_solver* s, int n_steps, int record, int graph, float* ms);

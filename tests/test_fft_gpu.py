@@ -12,7 +12,9 @@ pytestmark = pytest.mark.gpu
 # the operator-test shapes of the reference padded to 2/3/5-smooth sizes,
 # odd/even mixes, 1-D and 2-D embeddings, the radix-3/5 config sizes
 SHAPES = [(8, 8, 8), (8, 9, 6), (6, 6, 8), (9, 8, 8), (1, 1, 600), (1, 20, 24), (16, 24, 30), (5, 12, 10),
-          (3, 25, 9), (96, 96, 128), (40, 48, 64), (64, 80, 96), (20, 24, 320)]
+          (3, 25, 9), (96, 96, 128), (40, 48, 64), (64, 80, 96), (20, 24, 320),
+          # every axis on the size-specialised path
+          (16, 24, 32), (32, 48, 48), (8, 16, 256), (160, 16, 8), (24, 192, 16), (128, 64, 24)]
 
 
 def _rel(a, b):

@@ -12,7 +12,9 @@ from oracle import kspace as ok
 pytestmark = pytest.mark.gpu
 
 CASES = [((12, 10, 16), False, True), ((9, 12, 10), True, True), ((16, 16, 24), True, False), ((1, 1, 40), False, True),
-         ((1, 18, 20), True, True), ((48, 40, 64), True, True)]
+         ((1, 18, 20), True, True), ((48, 40, 64), True, True),
+         # every axis on the size-specialised path
+         ((32, 32, 32), True, True), ((24, 48, 96), False, True), ((16, 64, 48), True, False)]
 
 
 def _setup(shape, nonlinear, hetero, seed=0):
