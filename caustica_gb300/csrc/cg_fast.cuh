@@ -237,11 +237,11 @@ struct RowEx {
   __device__ __forceinline__ float2& at(int k1, int n2) const { return base[k1 * LD + n2]; }
 };
 
-template <int A, int B>
+template <int A, int B, int P = 16>
 struct ColEx {
   float2* base;  // + lane pencil
   static constexpr int SLAB = 0;
-  __device__ __forceinline__ float2& at(int k1, int n2) const { return base[(k1 * B + n2) * 16]; }
+  __device__ __forceinline__ float2& at(int k1, int n2) const { return base[(k1 * B + n2) * P]; }
 };
 
 // Twiddle table of an (A, B) transform in the order the threads read it:

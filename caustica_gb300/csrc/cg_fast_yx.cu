@@ -8,11 +8,21 @@
 #include "cg_fast.cuh"
 #include "cg_kspace.cuh"
 
-// resident CTAs per SM the register allocation targets
-#ifndef CG_FAST_MINB_YX
-#define CG_FAST_MINB_YX 3
+// resident CTAs per SM the register allocation targets (y: 8-row CTAs,
+// x: 16-column CTAs; both ~85 registers per thread)
+#ifndef CG_FAST_MINB_Y
+#define CG_FAST_MINB_Y 6
 #endif
-#define CG_FAST_MINB CG_FAST_MINB_YX
+#ifndef CG_FAST_MINB_X
+#define CG_FAST_MINB_X 3
+#endif
+// rows per y-CTA and columns per x-CTA (16 threads each)
+#ifndef CG_YP
+#define CG_YP 8
+#endif
+#ifndef CG_XP
+#define CG_XP 16
+#endif
 
 using cgf::ColEx;
 using cgf::RowEx;
@@ -21,7 +31,7 @@ using cgf::fft2;
 using cgf::static_for;
 
 template <int N>
-__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_ypass(int mode, Dims d, Tables t, float2* __restrict__ S0,
+__global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(int mode, Dims d, Tables t, float2* __restrict__ S0,
                                                          float2* __restrict__ S1, float2* __restrict__ S2) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
   using Ex = RowEx<A, B>;
@@ -31,7 +41,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_ypass(int mode, D
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
   const Ex ex{sm + N + p * Ex::SLAB};
   const long long nrows = (long long)d.nx * d.nzh;
-  const long long row = (long long)blockIdx.x * CG_TILE + p;
+  const long long row = (long long)blockIdx.x * CG_YP + p;
   const bool valid = row < nrows;
   const long long off = (long long)blockIdx.y * d.nspec + row * N;
   __syncthreads();
@@ -91,7 +101,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_ypass(int mode, D
 }
 
 template <int N>
-__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_xpass(int mode, Dims d, Tables t, float kcoef, float invN,
+__global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(int mode, Dims d, Tables t, float kcoef, float invN,
                                                          float2* __restrict__ S0, float2* __restrict__ S1,
                                                          float2* __restrict__ S2) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
@@ -100,11 +110,11 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_xpass(int mode, D
   float2* twi = sm + N;  // (B, A) order
   cgf::fill_twt<A, B>(tw, t.twx);
   cgf::fill_twt<B, A>(twi, t.twx);
-  const int c = threadIdx.x & 15, s = threadIdx.x >> 4;
-  const ColEx<A, B> exf{sm + 2 * N + c};
-  const ColEx<B, A> exi{sm + 2 * N + c};
+  const int c = threadIdx.x % CG_XP, s = threadIdx.x / CG_XP;
+  const ColEx<A, B, CG_XP> exf{sm + 2 * N + c};
+  const ColEx<B, A, CG_XP> exi{sm + 2 * N + c};
   const long long ncol = (long long)d.nzh * d.ny;
-  const long long col = (long long)blockIdx.x * CG_TILE + c;
+  const long long col = (long long)blockIdx.x * CG_XP + c;
   const bool valid = col < ncol;
   const long long base = (long long)blockIdx.y * d.nspec + col;
   float kyz2 = 0.f;
@@ -175,20 +185,20 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_xpass(int mode, D
 
 template <int N>
 static size_t smem_y() {
-  return sizeof(float2) * (N + CG_TILE * RowEx<Split<N>::A, Split<N>::B>::SLAB);
+  return sizeof(float2) * (N + CG_YP * RowEx<Split<N>::A, Split<N>::B>::SLAB);
 }
 template <int N>
 static size_t smem_x() {
-  return sizeof(float2) * (2 * N + (size_t)N * CG_TILE);
+  return sizeof(float2) * (2 * N + (size_t)N * CG_XP);
 }
 
 bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1, float2* S2, int batch,
                 cudaStream_t st) {
-  const dim3 grid((unsigned)((d.nx * (long long)d.nzh + CG_TILE - 1) / CG_TILE), batch);
+  const dim3 grid((unsigned)((d.nx * (long long)d.nzh + CG_YP - 1) / CG_YP), batch);
   switch (d.ny) {
 #define CASE(n)                                                                   \
   case n:                                                                         \
-    kf_ypass<n><<<grid, CG_THREADS, smem_y<n>(), st>>>(mode, d, t, S0, S1, S2); \
+    kf_ypass<n><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(mode, d, t, S0, S1, S2); \
     return true;
     CG_FAST_SIZES(CASE)
 #undef CASE
@@ -199,11 +209,11 @@ bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1
 
 bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float invN, float2* S0, float2* S1,
                 float2* S2, int batch, cudaStream_t st) {
-  const dim3 grid((unsigned)(((long long)d.nzh * d.ny + CG_TILE - 1) / CG_TILE), batch);
+  const dim3 grid((unsigned)(((long long)d.nzh * d.ny + CG_XP - 1) / CG_XP), batch);
   switch (d.nx) {
 #define CASE(n)                                                                                    \
   case n:                                                                                          \
-    kf_xpass<n><<<grid, CG_THREADS, smem_x<n>(), st>>>(mode, d, t, kcoef, invN, S0, S1, S2); \
+    kf_xpass<n><<<grid, 16 * CG_XP, smem_x<n>(), st>>>(mode, d, t, kcoef, invN, S0, S1, S2); \
     return true;
     CG_FAST_SIZES(CASE)
 #undef CASE
