@@ -64,6 +64,12 @@ def _dist():
     return None, 0, 1, 0
 
 
+def replica_value(cells: int, steps: int, world_size: int, max_ms: float) -> float:
+    """Whole-job cell-steps/s of `world_size` independent replicas timed by
+    the slowest rank."""
+    return world_size * cells * steps / (max_ms * 1e-3)
+
+
 def _barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -265,7 +271,7 @@ def run_gb300(args, dist, rank, ws, local):
         dev.synchronize()
         _barrier(dist)
         t_ms = _max_over_ranks(dist, ms.value)
-        value = ws * ncell * K / (t_ms * 1e-3)
+        value = replica_value(ncell, K, ws, t_ms)
         # per-launch profile (events between launches)
         prof = np.zeros(8, np.float32)
         P = 2 * plan.spp

@@ -91,6 +91,7 @@ SIGNATURES = {
     "cg_pennes_create": [C.POINTER(PennesConfig), C.POINTER(_P)],
     "cg_pennes_destroy": [_P],
     "cg_pennes_set_coefficients": [_P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "cg_pennes_set_labels": [_P, _P, _I, _P, C.c_float, _I, _I, _P],
     "cg_pennes_set_state": [_P, _P, _P, _P],
     "cg_pennes_run": [_P, _I],
     "cg_pennes_check_finite": [_P, _P],

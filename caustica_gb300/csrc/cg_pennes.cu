@@ -29,7 +29,19 @@ struct PennesDev {
   const float* poff;
   int dirichlet, dose;
   float theta_wall, t_ref, half_dt_min;
+  // label mode: per-material (k, dt_sub/(rho C), w_b rho_b C_b, perfusion offset)
+  const uint8_t* labels;
+  const float4* ltab;
+  float inv_dx2;
+  int has_poff;
+  int wall_axes;  // label mode: bit a set when axis a has Dirichlet walls
 };
+
+// Harmonic-mean face conductance over dx^2 with the reference's float32
+// operation order: ((2 lo) hi / (lo + hi)) inv_dx2 (pennes.py:404-412).
+__device__ __forceinline__ float face_k(float lo, float hi, float inv_dx2) {
+  return __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(2.0f, lo), hi), __fadd_rn(lo, hi)), inv_dx2);
+}
 
 __device__ __forceinline__ float cem43_rate_dev(float T) {
   // R^(43 - T) with R = 0.5 above 43 C, 0.25 at or below (dose.py:74-89):
@@ -40,7 +52,12 @@ __device__ __forceinline__ float cem43_rate_dev(float T) {
 
 __global__ void k_pennes_step(PennesDev P, const float* __restrict__ th, float* __restrict__ thn, float* thmax,
                               float* dose, float* dcomp) {
+  __shared__ float4 tab[256];
+  if (P.labels)
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) tab[i] = P.ltab[i];
+  __syncthreads();
   const long long ncell = (long long)P.nx * P.ny * P.nz;
+  const long long sx = (long long)P.ny * P.nz, sy = P.nz;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ncell;
        i += (long long)gridDim.x * blockDim.x) {
     const int z = (int)(i % P.nz);
@@ -48,51 +65,70 @@ __global__ void k_pennes_step(PennesDev P, const float* __restrict__ th, float* 
     const int y = (int)(r % P.ny);
     const int x = (int)(r / P.ny);
     const float t0 = th[i];
+    const bool lab = P.labels != nullptr;
+    const float4 me = lab ? tab[P.labels[i]] : make_float4(0.f, 0.f, 0.f, 0.f);
     float w = 0.0f;
     // axis x: face above (x, x+1) then face below (x-1, x)
     if (x + 1 < P.nx) {
-      long long f = ((long long)x * P.ny + y) * P.nz + z;
-      w = __fadd_rn(w, __fmul_rn(__fsub_rn(th[i + (long long)P.ny * P.nz], t0), P.kfx[f]));
+      const float kf = lab ? face_k(me.x, tab[P.labels[i + sx]].x, P.inv_dx2)
+                           : P.kfx[((long long)x * P.ny + y) * P.nz + z];
+      w = __fadd_rn(w, __fmul_rn(__fsub_rn(th[i + sx], t0), kf));
     }
     if (x > 0) {
-      long long f = ((long long)(x - 1) * P.ny + y) * P.nz + z;
-      w = __fsub_rn(w, __fmul_rn(__fsub_rn(t0, th[i - (long long)P.ny * P.nz]), P.kfx[f]));
+      const float kf = lab ? face_k(tab[P.labels[i - sx]].x, me.x, P.inv_dx2)
+                           : P.kfx[((long long)(x - 1) * P.ny + y) * P.nz + z];
+      w = __fsub_rn(w, __fmul_rn(__fsub_rn(t0, th[i - sx]), kf));
     }
     if (y + 1 < P.ny) {
-      long long f = ((long long)x * (P.ny - 1) + y) * P.nz + z;
-      w = __fadd_rn(w, __fmul_rn(__fsub_rn(th[i + P.nz], t0), P.kfy[f]));
+      const float kf = lab ? face_k(me.x, tab[P.labels[i + sy]].x, P.inv_dx2)
+                           : P.kfy[((long long)x * (P.ny - 1) + y) * P.nz + z];
+      w = __fadd_rn(w, __fmul_rn(__fsub_rn(th[i + sy], t0), kf));
     }
     if (y > 0) {
-      long long f = ((long long)x * (P.ny - 1) + (y - 1)) * P.nz + z;
-      w = __fsub_rn(w, __fmul_rn(__fsub_rn(t0, th[i - P.nz]), P.kfy[f]));
+      const float kf = lab ? face_k(tab[P.labels[i - sy]].x, me.x, P.inv_dx2)
+                           : P.kfy[((long long)x * (P.ny - 1) + (y - 1)) * P.nz + z];
+      w = __fsub_rn(w, __fmul_rn(__fsub_rn(t0, th[i - sy]), kf));
     }
     if (z + 1 < P.nz) {
-      long long f = ((long long)x * P.ny + y) * (P.nz - 1) + z;
-      w = __fadd_rn(w, __fmul_rn(__fsub_rn(th[i + 1], t0), P.kfz[f]));
+      const float kf = lab ? face_k(me.x, tab[P.labels[i + 1]].x, P.inv_dx2)
+                           : P.kfz[((long long)x * P.ny + y) * (P.nz - 1) + z];
+      w = __fadd_rn(w, __fmul_rn(__fsub_rn(th[i + 1], t0), kf));
     }
     if (z > 0) {
-      long long f = ((long long)x * P.ny + y) * (P.nz - 1) + (z - 1);
-      w = __fsub_rn(w, __fmul_rn(__fsub_rn(t0, th[i - 1]), P.kfz[f]));
+      const float kf = lab ? face_k(tab[P.labels[i - 1]].x, me.x, P.inv_dx2)
+                           : P.kfz[((long long)x * P.ny + y) * (P.nz - 1) + (z - 1)];
+      w = __fsub_rn(w, __fmul_rn(__fsub_rn(t0, th[i - 1]), kf));
     }
     if (P.dirichlet) {
       const long long pyz = (long long)P.ny * P.nz, pxz = (long long)P.nx * P.nz, pxy = (long long)P.nx * P.ny;
       const float* W = P.walls;
       const float dwall = __fsub_rn(P.theta_wall, t0);
-      if (x == 0) w = __fadd_rn(w, __fmul_rn(W[(long long)y * P.nz + z], dwall));
-      if (x == P.nx - 1) w = __fadd_rn(w, __fmul_rn(W[pyz + (long long)y * P.nz + z], dwall));
-      W += 2 * pyz;
-      if (y == 0) w = __fadd_rn(w, __fmul_rn(W[(long long)x * P.nz + z], dwall));
-      if (y == P.ny - 1) w = __fadd_rn(w, __fmul_rn(W[pxz + (long long)x * P.nz + z], dwall));
-      W += 2 * pxz;
-      if (z == 0) w = __fadd_rn(w, __fmul_rn(W[(long long)x * P.ny + y], dwall));
-      if (z == P.nz - 1) w = __fadd_rn(w, __fmul_rn(W[pxy + (long long)x * P.ny + y], dwall));
+      // 2 k_edge / dx^2 (pennes.py:414-426); label mode: walls only on the grid's own axes
+      const float wk = lab ? __fmul_rn(__fmul_rn(2.0f, me.x), P.inv_dx2) : 0.f;
+      const bool wx = !lab || (P.wall_axes & 1), wy = !lab || (P.wall_axes & 2), wz = !lab || (P.wall_axes & 4);
+      if (wx && x == 0) w = __fadd_rn(w, __fmul_rn(lab ? wk : W[(long long)y * P.nz + z], dwall));
+      if (wx && x == P.nx - 1) w = __fadd_rn(w, __fmul_rn(lab ? wk : W[pyz + (long long)y * P.nz + z], dwall));
+      if (!lab) W += 2 * pyz;
+      if (wy && y == 0) w = __fadd_rn(w, __fmul_rn(lab ? wk : W[(long long)x * P.nz + z], dwall));
+      if (wy && y == P.ny - 1) w = __fadd_rn(w, __fmul_rn(lab ? wk : W[pxz + (long long)x * P.nz + z], dwall));
+      if (!lab) W += 2 * pxz;
+      if (wz && z == 0) w = __fadd_rn(w, __fmul_rn(lab ? wk : W[(long long)x * P.ny + y], dwall));
+      if (wz && z == P.nz - 1) w = __fadd_rn(w, __fmul_rn(lab ? wk : W[pxy + (long long)x * P.ny + y], dwall));
     }
     if (P.q) w = __fadd_rn(w, P.q[i]);
-    if (P.perf) {
-      w = __fsub_rn(w, __fmul_rn(P.perf[i], t0));
-      if (P.poff) w = __fsub_rn(w, P.poff[i]);
+    if (lab) {
+      if (me.z != 0.0f || P.has_poff) {
+        w = __fsub_rn(w, __fmul_rn(me.z, t0));
+        if (P.has_poff) w = __fsub_rn(w, me.w);
+      }
+      w = __fmul_rn(w, me.y);
+    } else {
+      if (P.perf) {
+        w = __fsub_rn(w, __fmul_rn(P.perf[i], t0));
+        if (P.poff) w = __fsub_rn(w, P.poff[i]);
+      }
+      w = __fmul_rn(w, P.coeff[i]);
     }
-    w = __fmul_rn(w, P.coeff[i]);
     const float t1 = __fadd_rn(t0, w);
     thn[i] = t1;
     const float tm = thmax[i];
@@ -130,6 +166,10 @@ struct cg_pennes {
   float *kfx = nullptr, *kfy = nullptr, *kfz = nullptr, *walls = nullptr;
   float *perf = nullptr, *coeff = nullptr, *q = nullptr, *poff = nullptr;
   int* flag = nullptr;
+  uint8_t* labels = nullptr;
+  float4* ltab = nullptr;
+  float inv_dx2 = 0.f;
+  int lab_poff = 0, wall_axes = 7;
   int has_coef = 0, has_state = 0;
   cudaStream_t stream = nullptr;
 };
@@ -137,7 +177,7 @@ struct cg_pennes {
 static void pennes_free(cg_pennes* h) {
   if (!h) return;
   void* ptrs[] = {h->th[0], h->th[1], h->thmax, h->dose, h->dcomp, h->kfx, h->kfy, h->kfz,
-                  h->walls, h->perf, h->coeff, h->q, h->poff, h->flag};
+                  h->walls, h->perf, h->coeff, h->q, h->poff, h->flag, h->labels, h->ltab};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -224,6 +264,28 @@ extern "C" int cg_pennes_set_coefficients(cg_pennes* h, const float* kf_x, const
   return CG_OK;
 }
 
+extern "C" int cg_pennes_set_labels(cg_pennes* h, const uint8_t* labels, int n_labels, const float* table,
+                                     float inv_dx2, int has_perf_offset, int wall_axes, const float* q) {
+  CG_REQUIRE(h && labels && table, "null argument");
+  CG_REQUIRE(n_labels >= 1 && n_labels <= 256, "n_labels must be 1..256, got %d", n_labels);
+  if (!h->labels) {
+    CG_CUDA_TRY(cudaMalloc((void**)&h->labels, (size_t)h->ncell));
+    CG_CUDA_TRY(cudaMalloc((void**)&h->ltab, 256 * sizeof(float4)));
+  }
+  float4 tab[256];
+  memset(tab, 0, sizeof(tab));
+  for (int i = 0; i < n_labels; ++i) tab[i] = make_float4(table[4 * i], table[4 * i + 1], table[4 * i + 2], table[4 * i + 3]);
+  CG_CUDA_TRY(cudaMemcpyAsync(h->labels, labels, (size_t)h->ncell, cudaMemcpyDefault, h->stream));
+  CG_CUDA_TRY(cudaMemcpyAsync(h->ltab, tab, sizeof(tab), cudaMemcpyHostToDevice, h->stream));
+  if (q) CG_CUDA_TRY(cudaMemcpyAsync(h->q, q, sizeof(float) * (size_t)h->ncell, cudaMemcpyDefault, h->stream));
+  CG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->inv_dx2 = inv_dx2;
+  h->lab_poff = has_perf_offset;
+  h->wall_axes = wall_axes;
+  h->has_coef = 1 | (q ? 4 : 0);
+  return CG_OK;
+}
+
 extern "C" int cg_pennes_set_state(cg_pennes* h, const float* theta, const float* theta_max, const float* dose) {
   CG_REQUIRE(h && theta && theta_max, "null argument");
   const size_t n = (size_t)h->ncell;
@@ -251,6 +313,11 @@ static PennesDev make_dev(const cg_pennes* h) {
   P.theta_wall = h->cfg.theta_wall;
   P.t_ref = h->cfg.t_ref;
   P.half_dt_min = h->cfg.half_dt_min;
+  P.labels = h->labels;
+  P.ltab = h->ltab;
+  P.inv_dx2 = h->inv_dx2;
+  P.has_poff = h->lab_poff;
+  P.wall_axes = h->wall_axes;
   return P;
 }
 

@@ -126,19 +126,19 @@ def _first_occurrence(inv: np.ndarray, n: int, chunk: int = 1 << 20) -> np.ndarr
     return first
 
 
-def label_medium(medium, max_labels: int = 256):
-    """Exact label decomposition of the four property volumes, or None.
+def label_volumes(vols, id_map=None, max_labels: int = 256):
+    """Exact label decomposition of equally shaped float32 volumes.
 
-    Returns ``(labels uint8, props (n, 4) float32)`` when the medium has at
-    most ``max_labels`` distinct (alpha, rho, c, beta) tuples.
+    Returns ``(labels uint8, props (n, len(vols)) float32)`` when at most
+    ``max_labels`` distinct value tuples occur (``props[labels] == vols``),
+    else None. An integer ``id_map`` is tried first (O(N)).
     """
-    vols = [np.ascontiguousarray(getattr(medium, k), np.float32) for k in ("alpha", "rho", "c", "beta")]
-    id_map = getattr(medium, "id_map", None)
+    vols = [np.ascontiguousarray(v, np.float32) for v in vols]
+    nv = len(vols)
     if id_map is not None:
         ids_flat = np.asarray(id_map).reshape(-1)
         lo, hi = int(ids_flat.min()), int(ids_flat.max())
         if hi - lo < (1 << 20):
-            # small integer range: O(N) relabel through a lookup table
             present = np.flatnonzero(np.bincount(ids_flat - lo, minlength=hi - lo + 1))
             if len(present) <= max_labels:
                 lut = np.zeros(hi - lo + 1, np.int64)
@@ -146,28 +146,35 @@ def label_medium(medium, max_labels: int = 256):
                 inv = lut[ids_flat - lo]
                 first = _first_occurrence(inv, len(present))
                 props = np.stack([v.reshape(-1)[first] for v in vols], axis=1)
-                ok = all(np.array_equal(props[inv, i], vols[i].reshape(-1)) for i in range(4))
-                if ok:
+                if all(np.array_equal(props[inv, i], vols[i].reshape(-1)) for i in range(nv)):
                     return inv.astype(np.uint8).reshape(vols[0].shape), props.astype(np.float32)
-    bits = [v.reshape(-1).view(np.uint32).astype(np.uint64) for v in vols]
+    flat = [v.reshape(-1) for v in vols]
+    if all(np.all(f == f[0]) for f in flat):
+        return (np.zeros(vols[0].shape, np.uint8),
+                np.array([[f[0] for f in flat]], np.float32))
+    bits = [f.view(np.uint32).astype(np.uint64) for f in flat]
     for b in bits:
         if len(np.unique(b[:: max(1, b.size // 4096)])) > max_labels:
             return None
-    k1 = (bits[0] << np.uint64(32)) | bits[1]
-    k2 = (bits[2] << np.uint64(32)) | bits[3]
-    u1, i1 = np.unique(k1, return_inverse=True)
-    if len(u1) > max_labels:
-        return None
-    u2, i2 = np.unique(k2, return_inverse=True)
-    if len(u2) > max_labels:
-        return None
-    u, inv = np.unique(i1.astype(np.int64) * len(u2) + i2, return_inverse=True)
+    keys = [(bits[i] << np.uint64(32)) | (bits[i + 1] if i + 1 < nv else np.uint64(0)) for i in range(0, nv, 2)]
+    code = None
+    for k in keys:
+        u, inv_k = np.unique(k, return_inverse=True)
+        if len(u) > max_labels:
+            return None
+        code = inv_k.astype(np.int64) if code is None else code * len(u) + inv_k
+    u, inv = np.unique(code, return_inverse=True)
     if len(u) > max_labels:
         return None
-    first = np.zeros(len(u), np.int64)
-    first[inv[::-1]] = np.arange(len(inv))[::-1]
-    props = np.stack([v.reshape(-1)[first] for v in vols], axis=1).astype(np.float32)
+    first = _first_occurrence(inv, len(u))
+    props = np.stack([f[first] for f in flat], axis=1).astype(np.float32)
     return inv.astype(np.uint8).reshape(vols[0].shape), props
+
+
+def label_medium(medium, max_labels: int = 256):
+    """Labels of the acoustic property volumes (alpha, rho, c, beta), or None."""
+    vols = [getattr(medium, k) for k in ("alpha", "rho", "c", "beta")]
+    return label_volumes(vols, getattr(medium, "id_map", None), max_labels)
 
 
 def _embed3(shape):

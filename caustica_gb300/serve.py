@@ -223,7 +223,8 @@ def run_thermal(req: Request, result) -> Any:
 class Server:
     """Continuous-batching CW solve server on one GPU."""
 
-    def __init__(self, hbm_budget_bytes: int | None = None, max_pack: int = 8, poll_s: float = 2e-4):
+    def __init__(self, hbm_budget_bytes: int | None = None, max_pack: int = 8, poll_s: float = 2e-4,
+                 thermal_workers: int = 3):
         if hbm_budget_bytes is None:
             hbm_budget_bytes = 200 << 30
         self.budget = int(hbm_budget_bytes)
@@ -238,9 +239,12 @@ class Server:
         self._thermal_q: queue.Queue = queue.Queue()
         self.stats = {"groups": 0, "packed_members": 0, "solo_reruns": 0, "peak_bytes": 0, "max_active": 0}
         self._thread = threading.Thread(target=self._loop, name="cg-serve", daemon=True)
-        self._tworker = threading.Thread(target=self._thermal_loop, name="cg-thermal", daemon=True)
+        # thermal phases run on their own handles and streams, so several overlap on the GPU
+        self._tworkers = [threading.Thread(target=self._thermal_loop, name=f"cg-thermal-{i}", daemon=True)
+                          for i in range(max(1, int(thermal_workers)))]
         self._thread.start()
-        self._tworker.start()
+        for t in self._tworkers:
+            t.start()
 
     # -------------------------------------------------------------- api --
     def submit(self, req: Request) -> Future:
@@ -256,8 +260,10 @@ class Server:
             self._lock.notify()
         if wait:
             self._thread.join()
-            self._thermal_q.put(None)
-            self._tworker.join()
+            for _ in self._tworkers:
+                self._thermal_q.put(None)
+            for t in self._tworkers:
+                t.join()
 
     def __enter__(self):
         return self

@@ -157,6 +157,26 @@ def _ax(a, axis, sl):
     return a[tuple(idx)]
 
 
+def _representative(medium):
+    """For a single-material medium, a grid of min(n, 3) cells per axis has
+    every distinct Gershgorin row of the full grid (corners, edges, faces,
+    interior), so the stable step computed on it is the full grid's, exactly."""
+    vols = [np.asarray(getattr(medium, a)) for a in ("k", "rho", "specific_heat", "perfusion")]
+    flat = [v.reshape(-1) for v in vols]
+    if not all(np.all(f == f[0]) for f in flat):
+        return None
+    shape = tuple(min(n, 3) for n in vols[0].shape)
+    return ThermalMedium(*(np.full(shape, f[0], np.float32) for f in flat), dx=medium.dx)
+
+
+def thermal_labels(medium, max_labels: int = 256):
+    """Exact label decomposition of (k, rho, C, w_b) or None (> max_labels materials)."""
+    from .engine import label_volumes
+
+    vols = [np.ascontiguousarray(getattr(medium, a), np.float32) for a in ("k", "rho", "specific_heat", "perfusion")]
+    return label_volumes(vols, getattr(medium, "id_map", None), max_labels)
+
+
 def _embed3(a: np.ndarray) -> np.ndarray:
     return a.reshape((1,) * (3 - a.ndim) + a.shape)
 
@@ -231,6 +251,9 @@ class PennesSolverGB300:
 
     def stable_dt(self, medium) -> float:
         """Gershgorin positivity bound (pennes.py:376-402)."""
+        small = _representative(medium)
+        if small is not None:
+            medium = small
         k = np.asarray(medium.k, np.float32)
         walls = self._walls(k, medium.dx) if self.boundary == "dirichlet" else None
         return self._stable(medium, self._faces(k, medium.dx), walls, self._perf(medium), self._inv_rho_c(medium))
@@ -295,20 +318,36 @@ class PennesSolverGB300:
             raise ValueError("temperature0 contains non-finite values; a solve cannot start from a field that is "
                              "not a temperature.")
         q_arr, q_kind = self._prepare_q(q, medium)
-        k = np.asarray(medium.k, np.float32)
-        faces = self._faces(k, medium.dx)
-        walls = self._walls(k, medium.dx) if self.boundary == "dirichlet" else None
-        perf = self._perf(medium)
         perfused = bool(medium.is_perfused)
-        inv_rho_c = self._inv_rho_c(medium)
-        dt_stable = self._stable(medium, faces, walls, perf, inv_rho_c)
-        n_sub = self._resolve_substeps(dt, dt_stable, medium)
-        dt_sub = dt / n_sub
-        coeff = (inv_rho_c * np.float32(dt_sub)).astype(np.float32)
         ref_minus_ta = np.float32(self.reference_temperature_c - self.arterial_temperature_c)
-        perf_offset = ((perf * ref_minus_ta).astype(np.float32)
-                       if perfused and float(ref_minus_ta) != 0.0 else None)
         theta_wall = np.float32(self.boundary_temperature_c) - t_ref
+        lab = thermal_labels(medium)
+        if lab is not None:
+            # per-material coefficients with the reference's float32 arithmetic
+            lab_vol, props = lab
+            pm = ThermalMedium(props[:, 0], props[:, 1], props[:, 2], props[:, 3], dx=medium.dx)
+            dt_stable = self.stable_dt(medium)
+            n_sub = self._resolve_substeps(dt, dt_stable, medium)
+            dt_sub = dt / n_sub
+            perf_l = self._perf(pm)
+            coeff_l = (self._inv_rho_c(pm) * np.float32(dt_sub)).astype(np.float32)
+            poff_l = ((perf_l * ref_minus_ta).astype(np.float32) if perfused and float(ref_minus_ta) != 0.0
+                      else np.zeros_like(perf_l))
+            table = np.ascontiguousarray(np.stack([props[:, 0], coeff_l, perf_l if perfused else 0 * perf_l,
+                                                   poff_l], axis=1).astype(np.float32))
+            faces = walls = perf = coeff = perf_offset = None
+        else:
+            k = np.asarray(medium.k, np.float32)
+            faces = self._faces(k, medium.dx)
+            walls = self._walls(k, medium.dx) if self.boundary == "dirichlet" else None
+            perf = self._perf(medium)
+            inv_rho_c = self._inv_rho_c(medium)
+            dt_stable = self._stable(medium, faces, walls, perf, inv_rho_c)
+            n_sub = self._resolve_substeps(dt, dt_stable, medium)
+            dt_sub = dt / n_sub
+            coeff = (inv_rho_c * np.float32(dt_sub)).astype(np.float32)
+            perf_offset = ((perf * ref_minus_ta).astype(np.float32)
+                           if perfused and float(ref_minus_ta) != 0.0 else None)
         dose_arr = None
         if dose:
             dose_arr = (np.zeros(shape, np.float32) if dose0 is None
@@ -320,7 +359,7 @@ class PennesSolverGB300:
         nd = len(shape)
         s3 = (1,) * (3 - nd) + shape
         kf3 = [None, None, None]
-        for ax, kf in enumerate(faces):
+        for ax, kf in enumerate(faces or []):
             kf3[3 - nd + ax] = np.ascontiguousarray(_embed3(kf))
         wall_buf = None
         if walls is not None:
@@ -338,7 +377,7 @@ class PennesSolverGB300:
             wall_buf = np.ascontiguousarray(np.concatenate(parts))
         cfg = _lib.PennesConfig()
         cfg.nx, cfg.ny, cfg.nz = s3
-        cfg.dirichlet = int(walls is not None)
+        cfg.dirichlet = int(self.boundary == "dirichlet")
         cfg.dose = int(dose)
         cfg.theta_wall = float(theta_wall)
         cfg.t_ref = float(t_ref)
@@ -347,10 +386,16 @@ class PennesSolverGB300:
         h = C.c_void_p()
         _lib.check(lib.cg_pennes_create(C.byref(cfg), C.byref(h)), "cg_pennes_create")
         try:
-            _lib.call("cg_pennes_set_coefficients", h, _lib.ptr(kf3[0]), _lib.ptr(kf3[1]), _lib.ptr(kf3[2]),
-                      _lib.ptr(wall_buf), _lib.ptr(np.ascontiguousarray(perf)) if perfused else None,
-                      _lib.ptr(np.ascontiguousarray(coeff)), _lib.ptr(q_arr),
-                      _lib.ptr(np.ascontiguousarray(perf_offset)) if perf_offset is not None else None)
+            if lab is not None:
+                wall_axes = sum(1 << a for a in range(3 - nd, 3))
+                _lib.call("cg_pennes_set_labels", h, _lib.ptr(np.ascontiguousarray(lab_vol.reshape(s3))),
+                          len(table), _lib.ptr(table), float(np.float32(1.0 / (medium.dx * medium.dx))),
+                          int(perfused and float(ref_minus_ta) != 0.0), wall_axes, _lib.ptr(q_arr))
+            else:
+                _lib.call("cg_pennes_set_coefficients", h, _lib.ptr(kf3[0]), _lib.ptr(kf3[1]), _lib.ptr(kf3[2]),
+                          _lib.ptr(wall_buf), _lib.ptr(np.ascontiguousarray(perf)) if perfused else None,
+                          _lib.ptr(np.ascontiguousarray(coeff)), _lib.ptr(q_arr),
+                          _lib.ptr(np.ascontiguousarray(perf_offset)) if perf_offset is not None else None)
             theta = np.ascontiguousarray(theta, np.float32)
             _lib.call("cg_pennes_set_state", h, _lib.ptr(theta), _lib.ptr(theta), _lib.ptr(dose_arr))
             samples, times = [], []
@@ -409,4 +454,4 @@ class PennesSolverGB300:
                   "blood_density": self.blood_density, "blood_specific_heat": self.blood_specific_heat,
                   "arterial_temperature_c": self.arterial_temperature_c,
                   "reference_temperature_c": self.reference_temperature_c, "dose_accumulated": dose,
-                  "dose_summation": "kahan"})
+                  "dose_summation": "kahan", "coefficients": "labels" if lab is not None else "dense"})

@@ -171,6 +171,14 @@ int cg_pennes_destroy(cg_pennes* h);
 int cg_pennes_set_coefficients(cg_pennes* h, const float* kf_x, const float* kf_y, const float* kf_z,
                                const float* walls, const float* perf, const float* coeff, const float* q,
                                const float* perf_offset);
+/* Coefficients as a uint8 material label volume [cells] plus n_labels rows
+ * (k, dt_sub/(rho C), w_b rho_b C_b, perfusion offset); the kernel forms the
+ * harmonic-mean faces ((2 k_i) k_j / (k_i + k_j)) inv_dx2 and the Dirichlet
+ * walls (2 k) inv_dx2 in float32 in the reference's order (pennes.py:404-447).
+ * wall_axes: bit a set when axis a carries walls. q [cells] may be NULL.
+ * Replaces cg_pennes_set_coefficients. */
+int cg_pennes_set_labels(cg_pennes* h, const uint8_t* labels, int n_labels, const float* table, float inv_dx2,
+                         int has_perf_offset, int wall_axes, const float* q);
 /* State (host or device): theta = T - t_ref, theta_max, dose, and the
  * dose-rate carry; dose/dose_comp may be NULL when dose is off. */
 int cg_pennes_set_state(cg_pennes* h, const float* theta, const float* theta_max, const float* dose);

@@ -139,3 +139,26 @@ def test_thermal_result_chain_refuses_an_unchained_dose():
     b = th.ThermalResult(np.zeros(3), np.zeros(3), np.zeros(3), [], [], 1.0, 1, 1.0, 1)
     with pytest.raises(ValueError, match="not chained"):
         th.ThermalResult.chain([a, b])
+
+
+def test_stable_step_of_a_single_material_from_the_small_grid_equals_the_full_grid():
+    for boundary in ("insulated", "dirichlet"):
+        s = th.PennesSolverGB300(boundary=boundary)
+        for shape in ((9, 8, 7), (2, 5, 6), (12, 4)):
+            tm = th.ThermalMedium.homogeneous(shape, k=0.52, rho=1045.0, specific_heat=3580.0, perfusion=3e-3,
+                                              dx=0.25e-3)
+            k = np.asarray(tm.k, np.float32)
+            walls = s._walls(k, tm.dx) if boundary == "dirichlet" else None
+            full = s._stable(tm, s._faces(k, tm.dx), walls, s._perf(tm), s._inv_rho_c(tm))
+            assert s.stable_dt(tm) == full
+
+
+def test_thermal_label_decomposition_is_exact():
+    g = load_golden("pennes3d_insulated")
+    ids = np.random.default_rng(2).integers(0, 3, g["k"].shape)
+    vals = {0: (0.5, 1000.0, 3600.0, 0.0), 1: (0.4, 950.0, 3400.0, 2e-3), 2: (0.55, 1050.0, 3700.0, 5e-3)}
+    vols = [np.vectorize(lambda i, j=j: vals[int(i)][j])(ids).astype(np.float32) for j in range(4)]
+    tm = th.ThermalMedium(*vols, dx=1e-3)
+    lab, props = th.thermal_labels(tm)
+    for j, v in enumerate(vols):
+        np.testing.assert_array_equal(props[lab, j], v)

@@ -80,3 +80,26 @@ def test_an_overflowing_dose_is_caught_by_the_same_guard():
     tm = cg.ThermalMedium.homogeneous(shape, k=0.5, rho=1050.0, specific_heat=3600.0, perfusion=0.0, dx=1e-3)
     with pytest.raises(cg.thermal.ThermalDivergedError, match="CEM43 dose"):
         cg.PennesSolverGB300().solve(np.full(shape, 37.0, np.float32), 2.0e6, tm, 1.0, 400, dose=True)
+
+
+@pytest.mark.parametrize("shape,boundary,tref", [((10, 9, 12), "insulated", None), ((9, 11, 8), "dirichlet", 36.0),
+                                                 ((14, 12), "dirichlet", None), ((12, 10), "insulated", 38.0)])
+def test_label_coefficients_equal_the_reference_float32_path(shape, boundary, tref):
+    rng = np.random.default_rng(sum(shape))
+    ids = rng.integers(0, 3, shape)
+    vals = {0: (0.5, 1000.0, 3600.0, 0.0), 1: (0.4, 950.0, 3400.0, 2e-3), 2: (0.55, 1050.0, 3700.0, 5e-3)}
+    vols = [np.vectorize(lambda i, j=j: vals[int(i)][j])(ids).astype(np.float32) for j in range(4)]
+    tm = cg.ThermalMedium(*vols, dx=0.3e-3)
+    q = (rng.random(shape) ** 3 * 4e6).astype(np.float32)
+    t0 = (37.0 + rng.uniform(0, 3, shape)).astype(np.float32)
+    s = cg.PennesSolverGB300(boundary=boundary, reference_temperature_c=tref, on_unstable="substep")
+    res = s.solve(t0, q, tm, dt=0.05, n_steps=30, dose=True)
+    assert res.meta["coefficients"] == "labels"
+    kw = dict(k=vols[0], rho=vols[1], specific_heat=vols[2], perfusion=vols[3], dx=tm.dx, dt=0.05, n_steps=30,
+              dose=True, boundary=boundary, reference_temperature_c=tref, on_unstable="substep")
+    ref32 = op.solve(t0, q, dtype=np.float32, **kw)
+    np.testing.assert_array_equal(res.temperature, ref32["temperature"])
+    ref64 = op.solve(t0, q, dtype=np.float64, **kw)
+    assert np.abs(res.temperature - ref64["temperature"]).max() < T_TOL
+    rel = np.abs(res.dose_cem43 - ref64["dose_cem43"]) / np.maximum(np.abs(ref64["dose_cem43"]), 1e-30)
+    assert rel.max() < DOSE_TOL
