@@ -4,7 +4,8 @@ A drop-in for caustica's ``linear``/``westervelt`` solvers and its
 ``PennesSolver``: the host code here mirrors the reference interfaces and
 calls ``libcaustica_gb300.so`` (C ABI, ``include/caustica_gb300.h``) through
 ctypes. Every time step runs in hand-written CUDA kernels; there is no CPU
-fallback.
+fallback. The focal metrics (``report/metrics.py``) and the heating source
+(``sensors.py``) of a result are reduced on the GPU as well.
 """
 
 from .contract import (
@@ -17,12 +18,14 @@ from .contract import (
     SolverDivergedError,
     SolverResult,
 )
+from .metrics import FieldFrame, device_focus_metrics, focus_metrics
+from .sensors import HeatingSource
 from .solvers import LinearKSpaceGB300, WesterveltKSpaceGB300, get
 from .thermal import PennesSolverGB300, ThermalMedium, ThermalResult
 
 __all__ = [
     "CWRunSpec", "CWSource", "Grid", "Medium", "PMLSpec", "SolverCapabilityError", "SolverDivergedError",
     "SolverResult", "LinearKSpaceGB300", "WesterveltKSpaceGB300", "get", "PennesSolverGB300", "ThermalMedium",
-    "ThermalResult",
+    "ThermalResult", "FieldFrame", "focus_metrics", "device_focus_metrics", "HeatingSource",
 ]
 __version__ = "0.1.0"

@@ -55,6 +55,33 @@ class PennesConfig(C.Structure):
     ]
 
 
+class FocusInput(C.Structure):
+    _fields_ = [
+        ("p1", C.c_void_p), ("p2", C.c_void_p), ("pmax", C.c_void_p),
+        ("shape", C.c_int * 3), ("lo", C.c_int * 3), ("hi", C.c_int * 3), ("probe", C.c_int * 3),
+        ("offset", C.c_int * 3), ("dx", C.c_double),
+    ]
+
+
+class FocusReport(C.Structure):
+    _fields_ = [
+        ("peak", C.c_longlong), ("p_peak", C.c_float), ("p_max_at_peak", C.c_float),
+        ("n_above_half", C.c_longlong), ("p_probe", C.c_float), ("has_a2", C.c_int),
+        ("a2_at_peak", C.c_float), ("a2_peak", C.c_float), ("a2_peak_index", C.c_longlong),
+        ("truncated", C.c_int * 3), ("left", C.c_double * 3), ("right", C.c_double * 3),
+    ]
+
+
+class HeatingSpec(C.Structure):
+    _fields_ = [
+        ("n_terms", C.c_int), ("harmonics", C.c_int * 8), ("phasor", C.c_void_p * 8), ("shape", C.c_int * 3),
+        ("n_labels", C.c_int), ("coef", C.c_void_p), ("labels", C.c_void_p),
+        ("alpha", C.c_void_p), ("rho", C.c_void_p), ("c", C.c_void_p), ("alpha_factor", C.c_double * 8),
+        ("map_shape", C.c_int * 3), ("map_origin", C.c_int * 3),
+        ("q_shape", C.c_int * 3), ("q_origin", C.c_int * 3), ("scale", C.c_float),
+    ]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _LL = C.c_longlong
@@ -96,6 +123,13 @@ SIGNATURES = {
     "cg_pennes_run": [_P, _I],
     "cg_pennes_check_finite": [_P, _P],
     "cg_pennes_get_state": [_P, _P, _P, _P],
+    "cg_focus_metrics": [C.POINTER(FocusInput), C.POINTER(FocusReport), _P],
+    "cg_solver_focus_metrics": [_P, _I, C.POINTER(FocusInput), C.POINTER(FocusReport)],
+    "cg_heating_q": [C.POINTER(HeatingSpec), _P, _P, _P],
+    "cg_solver_heating_q": [_P, _I, C.POINTER(HeatingSpec), _P, _P],
+    "cg_buffer_alloc": [C.c_size_t, C.POINTER(_P)],
+    "cg_buffer_free": [_P],
+    "cg_buffer_copy": [_P, _P, C.c_size_t],
 }
 _RESTYPE = {"cg_last_error": C.c_char_p}
 
@@ -145,3 +179,44 @@ def ptr(a: np.ndarray | None):
     if not a.flags.c_contiguous:
         raise ValueError("array must be C-contiguous")
     return a.ctypes.data_as(C.c_void_p)
+
+
+class DeviceArray:
+    """A device buffer of the library (``cg_buffer_alloc``) with a NumPy shape and dtype.
+
+    Carries fields between device calls without a host copy (phasors into
+    the focal metrics, Q into the Pennes step); ``to_host`` reads it back.
+    """
+
+    def __init__(self, shape, dtype):
+        self.shape = tuple(int(n) for n in shape)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape, dtype=np.int64)) * self.dtype.itemsize
+        h = C.c_void_p()
+        check(load().cg_buffer_alloc(self.nbytes, C.byref(h)), "cg_buffer_alloc")
+        self.ptr = h
+
+    @classmethod
+    def from_host(cls, a: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(a)
+        d = cls(a.shape, a.dtype)
+        if d.nbytes:
+            call("cg_buffer_copy", d.ptr, ptr(a), d.nbytes)
+        return d
+
+    def to_host(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        if self.nbytes:
+            call("cg_buffer_copy", ptr(out), self.ptr, self.nbytes)
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            load().cg_buffer_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass

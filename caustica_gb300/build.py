@@ -23,7 +23,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libcaustica_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["cg_kspace.cu", "cg_pennes.cu", "cg_fast_yx.cu", "cg_fast_z.cu"]
+SOURCES = ["cg_kspace.cu", "cg_pennes.cu", "cg_fast_yx.cu", "cg_fast_z.cu", "cg_post.cu"]
 
 
 def nvcc() -> str:
@@ -34,7 +34,9 @@ def nvcc() -> str:
 
 
 def _flags(verbose_ptxas: bool = False) -> list[str]:
+    # host code keeps the reference's operation order: no fused multiply-add
     f = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-ffp-contract=off",
          f"-I{INCLUDE}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
     if verbose_ptxas:
         f.append("-Xptxas=-v")

@@ -578,44 +578,7 @@ __global__ void k_advance(long long* ctl, long long by) { ctl[0] += by; }
 __global__ void k_set_ctl(long long* ctl, long long v) { ctl[0] = v; }
 
 // =============================================================== host ====
-struct cg_solver {
-  Dims d;
-  int B;
-  AxisPlan px, py, pz;
-  int spp, max_periods, nh, harm[CG_MAX_H];
-  double kcoef;
-  float invN;
-  int nonlinear;
-  // device memory
-  float* p = nullptr;
-  float* u = nullptr;
-  float2* S0 = nullptr;
-  float2* S1 = nullptr;
-  float2* S2 = nullptr;
-  float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
-  float *kx = nullptr, *ky = nullptr, *kz = nullptr, *kx2 = nullptr, *ky2 = nullptr, *kz2 = nullptr;
-  float *sx = nullptr, *sy = nullptr, *sz = nullptr;
-  uint8_t* labels = nullptr;
-  float4* ltab = nullptr;
-  float *dtr = nullptr, *rc2 = nullptr, *ab = nullptr, *b2 = nullptr;
-  int* src_ptr = nullptr;
-  int* src_z = nullptr;
-  float *src_ac = nullptr, *src_as = nullptr;
-  int n_src = 0;
-  float4* drive = nullptr;
-  int n_drive = 0;
-  float *bins = nullptr, *comp = nullptr, *pmax = nullptr;
-  unsigned int* peaks = nullptr;
-  int* harm_dev = nullptr;
-  long long* ctl = nullptr;
-  long long nrec = 0;
-  int rec_lo[3], rec_hi[3], conv_lo[3], conv_hi[3];
-  int has_medium = 0;
-  cudaStream_t stream = nullptr;
-  size_t smem_y = 0, smem_x = 0, smem_z = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one period, record off/on
-};
-
+#include "cg_solver.cuh"
 #include "caustica_gb300.h"
 
 static Tables make_tables(const cg_solver* s) {
@@ -698,7 +661,7 @@ static void solver_free(cg_solver* s) {
   void* ptrs[] = {s->p, s->u, s->S0, s->S1, s->S2, s->twx, s->twy, s->twz, s->kx, s->ky, s->kz, s->kx2, s->ky2,
                   s->kz2, s->sx, s->sy, s->sz, s->labels, s->ltab, s->dtr, s->rc2, s->ab, s->b2, s->src_ptr,
                   s->src_z, s->src_ac, s->src_as, s->drive, s->bins, s->comp, s->pmax, s->peaks, s->harm_dev,
-                  s->ctl};
+                  s->ctl, s->ph, s->post};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -1004,6 +967,7 @@ extern "C" int cg_solver_reset(cg_solver* s) {
   CG_CUDA_TRY(cudaMemsetAsync(s->peaks, 0, sizeof(unsigned int) * B * s->max_periods, st));
   CG_CUDA_TRY(cudaMemsetAsync(s->ctl, 0, sizeof(long long) * 2, st));
   CG_CUDA_TRY(cudaStreamSynchronize(st));
+  s->ph_valid = 0;
   return CG_OK;
 }
 
@@ -1102,6 +1066,7 @@ extern "C" int cg_solver_begin_record(cg_solver* s) {
   CG_CUDA_TRY(cudaMemsetAsync(s->bins, 0, sizeof(float) * nb, s->stream));
   CG_CUDA_TRY(cudaMemsetAsync(s->comp, 0, sizeof(float) * nb, s->stream));
   CG_CUDA_TRY(cudaMemsetAsync(s->pmax, 0, sizeof(float) * (size_t)s->B * s->nrec, s->stream));
+  s->ph_valid = 0;
   return CG_OK;
 }
 
@@ -1119,22 +1084,34 @@ extern "C" int cg_solver_finalize(cg_solver* s, int n_record_steps, float* phaso
   CG_REQUIRE(s, "null solver");
   CG_REQUIRE(s->bins, "no record window has run (call cg_solver_begin_record first)");
   CG_REQUIRE(n_record_steps >= 1, "n_record_steps must be >= 1");
-  float2* out = nullptr;
-  int rc = dev_alloc(&out, (size_t)s->B * s->nh * s->nrec);
-  if (rc != CG_OK) return rc;
-  k_finalize<<<1024, 256, 0, s->stream>>>(make_record(s), s->B, s->nh, s->harm_dev, n_record_steps, out);
+  if (!s->ph) {
+    int rc = dev_alloc(&s->ph, (size_t)s->B * s->nh * s->nrec);
+    if (rc != CG_OK) return rc;
+  }
+  k_finalize<<<1024, 256, 0, s->stream>>>(make_record(s), s->B, s->nh, s->harm_dev, n_record_steps, s->ph);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && phasors)
-    e = cudaMemcpyAsync(phasors, out, sizeof(float2) * (size_t)s->B * s->nh * s->nrec, cudaMemcpyDefault, s->stream);
+    e = cudaMemcpyAsync(phasors, s->ph, sizeof(float2) * (size_t)s->B * s->nh * s->nrec, cudaMemcpyDefault,
+                        s->stream);
   if (e == cudaSuccess && pmax)
     e = cudaMemcpyAsync(pmax, s->pmax, sizeof(float) * (size_t)s->B * s->nrec, cudaMemcpyDefault, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-  cudaFree(out);
   if (e != cudaSuccess) {
     cg_set_error("finalize: %s", cudaGetErrorString(e));
     return CG_ERR_CUDA;
   }
+  s->ph_valid = 1;
   return CG_OK;
+}
+
+int cg_solver_post_scratch(cg_solver* s, size_t bytes) {
+  if (s->post_bytes >= bytes) return CG_OK;
+  if (s->post) cudaFree(s->post);
+  s->post = nullptr;
+  s->post_bytes = 0;
+  int rc = dev_alloc((char**)&s->post, bytes);
+  if (rc == CG_OK) s->post_bytes = bytes;
+  return rc;
 }
 
 extern "C" int cg_solver_get_state(cg_solver* s, float* p, float* u) {

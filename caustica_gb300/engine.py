@@ -219,6 +219,7 @@ class Plan:
     ramp_periods: float
     labels: np.ndarray | None = None
     label_table: np.ndarray | None = None
+    label_props: np.ndarray | None = None  # (n, 4) float32 alpha, rho, c, beta per label
     dense: tuple | None = None
     label: str = ""
     meta: dict = field(default_factory=dict)
@@ -294,7 +295,7 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
     nonlinear_active = bool(nonlinear) and not bool((beta == 0).all())
 
     # medium: exact labels when few materials, else dense float32 maps
-    labels = table = dense = None
+    labels = table = dense = props = None
     lab = label_medium(medium)
     if lab is not None:
         lab_vol, props = lab
@@ -333,7 +334,8 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
         harmonics=harmonics, tof=tof, eff_min=eff_min, eff_max=eff_max, spec=spec, rec=rec, rec_lo=rec_lo,
         rec_hi=rec_hi, conv_lo=conv_lo, conv_hi=conv_hi, pml3=pml3, pml_edge=pml_edge, src_xyz=src_xyz,
         src_scale=src_scale, src_phase=np.asarray(source.phases, np.float32), amplitude=float(source.amplitude),
-        ramp_periods=float(source.ramp_periods), labels=labels, label_table=table, dense=dense,
+        ramp_periods=float(source.ramp_periods), labels=labels, label_table=table, label_props=props,
+        dense=dense,
         label=getattr(source, "label", ""),
     )
 

@@ -16,9 +16,12 @@ scheduler thread
 * follows the reference's settle / record schedule per request
   (solvers/kspace/engine.py:484-557): periods are queued ahead as far as no
   convergence decision needs a period peak,
-* runs an attached Pennes / CEM43 phase (thermal/pennes.py:451-689) on a
-  second worker once the acoustic result is in, with Q = alpha |P1|^2/(rho c)
-  (sensors.py:259-273).
+* computes each request's focal metrics (report/metrics.py:192-313) and,
+  for a request with a thermal phase, its heating Q = sum alpha_n |P_n|^2 /
+  (rho c) (sensors.py:259-273) on the device from the handle's phasors,
+* runs the attached Pennes / CEM43 phase (thermal/pennes.py:451-689) on a
+  worker thread from that device Q: the field does not travel through the
+  host between the acoustic and the thermal solve.
 
 Each request's result is the one the plain solver returns for it alone: a
 packed member whose own convergence decisions differ from the shared
@@ -53,7 +56,9 @@ class Request:
     harmonics: tuple = (1,)
     record_region: tuple | None = None
     reference_point: tuple | None = None
-    thermal: dict | None = None  # {"medium", "dt", "n_heat", "n_cool", "T0"}
+    # {"medium", "dt", "n_heat", "n_cool", "T0", "q_scale", "harmonics", "alpha_power_law_y"}
+    thermal: dict | None = None
+    frame: Any = None  # a metrics.FieldFrame: focal metrics are computed when given
     tag: Any = None
 
 
@@ -66,6 +71,7 @@ class Outcome:
     t_done: float
     group_size: int
     member: int
+    metrics: dict | None = None
 
     @property
     def latency_s(self) -> float:
@@ -179,7 +185,8 @@ class _Group:
                           converged_period=sched[2], settle_capped=not sched[1], convergence_history=sched[3],
                           meta={"solver": p.name, "backend": "gb300", "padded_shape": p.padded, "c_ref": p.c_max,
                                 "nonlinear_active": p.nonlinear_active, "batch": len(self.items), "member": b})
-            out.append(_results(p, self.dev, ph, pm, common, b, _result_cls()))
+            res = _results(p, self.dev, ph, pm, common, b, _result_cls())
+            out.append((res, *_post_process(self.dev, b, res, self.items[b][0])))
         self.dev.close()
         return out
 
@@ -190,29 +197,49 @@ def _result_cls():
     return SolverResult
 
 
-def heating_q(phasor: np.ndarray, alpha, rho, c) -> np.ndarray:
-    """Q = alpha |P1|^2 / (rho c) in float64, returned float32 (sensors.py:259-273)."""
-    p2 = np.abs(np.asarray(phasor)).astype(np.float64) ** 2
-    q = np.asarray(alpha, np.float64) * p2 / (np.asarray(rho, np.float64) * np.asarray(c, np.float64))
-    return np.ascontiguousarray(q, np.float32)
+def _post_process(dev, member: int, result, req: Request):
+    """Focal metrics and heating Q of one member from the handle's device phasors."""
+    from .metrics import device_focus_metrics
+    from .sensors import HeatingSource
+
+    metrics = None
+    if req.frame is not None:
+        metrics = device_focus_metrics(dev, member, result, req.frame, source_amplitude=float(req.source.amplitude),
+                                       medium=req.medium)
+    heating = None
+    if req.thermal is not None:
+        th = req.thermal
+        heating = HeatingSource.from_solver(dev, member, result, req.medium, req.grid.dx,
+                                            harmonics=tuple(th.get("harmonics", (1,))),
+                                            alpha_power_law_y=th.get("alpha_power_law_y"),
+                                            scale=float(th.get("q_scale", 1.0)))
+    return metrics, heating
 
 
-def run_thermal(req: Request, result) -> Any:
-    """The attached heat-up + cool-down Pennes phases with the dose chained."""
+def run_thermal(req: Request, result, heating=None) -> Any:
+    """The attached heat-up + cool-down Pennes phases with the dose chained.
+
+    ``heating`` is the request's device Q on the grid (``_post_process``);
+    without it Q is formed on the device from ``result``'s phasors.
+    """
+    from .sensors import HeatingSource
     from .thermal import PennesSolverGB300, ThermalResult
 
     th = req.thermal
-    med = req.medium
-    region = result.region
-    q = np.zeros(req.grid.shape, np.float32)
-    q[region] = heating_q(result.phasor, med.alpha[region], med.rho[region], med.c[region])
-    q *= float(th.get("q_scale", 1.0))
+    if heating is None:
+        heating = HeatingSource.from_result(result, req.medium, req.grid.dx,
+                                            harmonics=tuple(th.get("harmonics", (1,))),
+                                            alpha_power_law_y=th.get("alpha_power_law_y"),
+                                            grid_shape=tuple(req.grid.shape), scale=float(th.get("q_scale", 1.0)))
     tmed = th["medium"]
     t0 = th.get("T0")
     if t0 is None:
         t0 = np.full(tmed.shape, 37.0, np.float32)
     solver = PennesSolverGB300(on_unstable="substep")
-    hot = solver.solve(t0, q, tmed, dt=th["dt"], n_steps=th["n_heat"], dose=True)
+    try:
+        hot = solver.solve(t0, heating, tmed, dt=th["dt"], n_steps=th["n_heat"], dose=True)
+    finally:
+        heating.close()
     if th.get("n_cool", 0):
         cool = solver.solve(hot.temperature, None, tmed, dt=th["dt"], n_steps=th["n_cool"], dose=True,
                             dose0=hot.dose_cem43)
@@ -340,17 +367,18 @@ class Server:
         finally:
             self._in_use -= g.bytes
         t = time.perf_counter()
-        for b, ((req, fut, ts), res) in enumerate(zip(g.items, results)):
-            if res is None:
+        for b, ((req, fut, ts), out) in enumerate(zip(g.items, results)):
+            if out is None:
                 self.stats["solo_reruns"] += 1
                 solo_req = Request(**{**req.__dict__})
                 with self._lock:
                     self._pending.appendleft((solo_req, fut, ts))
                 continue
+            res, metrics, heating = out
             oc = Outcome(result=res, thermal=None, t_submit=ts, t_admit=g.t_admit, t_done=t,
-                         group_size=len(g.items), member=b)
+                         group_size=len(g.items), member=b, metrics=metrics)
             if req.thermal is not None:
-                self._thermal_q.put((req, fut, oc))
+                self._thermal_q.put((req, fut, oc, heating))
             else:
                 fut.set_result(oc)
 
@@ -388,9 +416,9 @@ class Server:
             item = self._thermal_q.get()
             if item is None:
                 return
-            req, fut, oc = item
+            req, fut, oc, heating = item
             try:
-                oc.thermal = run_thermal(req, oc.result)
+                oc.thermal = run_thermal(req, oc.result, heating)
                 oc.t_done = time.perf_counter()
                 fut.set_result(oc)
             except Exception as exc:  # noqa: BLE001

@@ -23,6 +23,12 @@ import numpy as np
 
 from . import _lib
 
+
+def _qptr(q):
+    """Host or device pointer of the heating term (the library copies either)."""
+    return q.ptr if isinstance(q, _lib.DeviceArray) else _lib.ptr(q)
+
+
 log = logging.getLogger("caustica")
 
 BLOOD_DENSITY = 1050.0  # pennes.py:118
@@ -274,6 +280,17 @@ class PennesSolverGB300:
         if q is None:
             return None, "none"
         shape = medium.shape
+        if isinstance(q, _lib.DeviceArray):
+            # Q already on the device (cg_solver_heating_q / cg_heating_q)
+            if q.shape != tuple(shape) or q.dtype != np.float32:
+                raise ValueError(f"device Q is {q.dtype}{q.shape} but the thermal medium is float32{shape}.")
+            return q, "device"
+        dev = q.device_on(shape) if hasattr(q, "device_on") else None
+        if dev is not None:
+            if abs(q.dx - medium.dx) > 1e-12 * max(q.dx, medium.dx):
+                raise ValueError(f"the HeatingSource was built on a grid with dx = {q.dx * 1e3:.6g} mm but this "
+                                 f"thermal medium has dx = {medium.dx * 1e3:.6g} mm.")
+            return dev, f"HeatingSource({q.alpha_model}, device)"
         if hasattr(q, "q") and hasattr(q, "dx") and hasattr(q, "region"):
             if abs(q.dx - medium.dx) > 1e-12 * max(q.dx, medium.dx):
                 raise ValueError(f"the HeatingSource was built on a grid with dx = {q.dx * 1e3:.6g} mm but this "
@@ -390,11 +407,11 @@ class PennesSolverGB300:
                 wall_axes = sum(1 << a for a in range(3 - nd, 3))
                 _lib.call("cg_pennes_set_labels", h, _lib.ptr(np.ascontiguousarray(lab_vol.reshape(s3))),
                           len(table), _lib.ptr(table), float(np.float32(1.0 / (medium.dx * medium.dx))),
-                          int(perfused and float(ref_minus_ta) != 0.0), wall_axes, _lib.ptr(q_arr))
+                          int(perfused and float(ref_minus_ta) != 0.0), wall_axes, _qptr(q_arr))
             else:
                 _lib.call("cg_pennes_set_coefficients", h, _lib.ptr(kf3[0]), _lib.ptr(kf3[1]), _lib.ptr(kf3[2]),
                           _lib.ptr(wall_buf), _lib.ptr(np.ascontiguousarray(perf)) if perfused else None,
-                          _lib.ptr(np.ascontiguousarray(coeff)), _lib.ptr(q_arr),
+                          _lib.ptr(np.ascontiguousarray(coeff)), _qptr(q_arr),
                           _lib.ptr(np.ascontiguousarray(perf_offset)) if perf_offset is not None else None)
             theta = np.ascontiguousarray(theta, np.float32)
             _lib.call("cg_pennes_set_state", h, _lib.ptr(theta), _lib.ptr(theta), _lib.ptr(dose_arr))

@@ -275,7 +275,9 @@ def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear:
     radius 0.3x the lateral interior, ROC 0.6x the axial extent, apex two
     cells inside the sponge), and a medium drawn from a small pool for
     ``p_reuse`` of the requests (those can be packed into one launch).
-    Schedule: flight time to the focus + 4 periods, 2 recorded periods."""
+    Schedule: flight time to the focus + 4 periods, 2 recorded periods.
+    Every request asks for its focal metrics (apex and geometric focus)."""
+    from .metrics import FieldFrame
     from .serve import Request
     from .thermal import ThermalMedium
 
@@ -307,7 +309,8 @@ def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear:
             th = {"medium": ThermalMedium.homogeneous(shape, k=0.5, rho=1000.0, specific_heat=3600.0,
                                                       perfusion=0.5 / 1050.0, dx=dx),
                   "dt": 0.05, "n_heat": 400, "n_cool": 1200}
+        frame = FieldFrame(dx=dx, grid_shape=shape, pml_vox=pml, apex_vox=apex, focus_vox=focus)
         reqs.append(Request(grid=grid, medium=med, source=src, spec=spec, nonlinear=nonlinear,
-                            harmonics=(1, 2) if nonlinear else (1,), reference_point=focus, thermal=th,
+                            harmonics=(1, 2) if nonlinear else (1,), reference_point=focus, thermal=th, frame=frame,
                             tag={"i": i, "shape": shape, "nonlinear": nonlinear, "thermal": thermal}))
     return reqs

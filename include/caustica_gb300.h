@@ -13,6 +13,7 @@
 #ifndef CAUSTICA_GB300_H
 #define CAUSTICA_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -188,6 +189,93 @@ int cg_pennes_run(cg_pennes* h, int n_sub);
  * (pennes.py:756-781). */
 int cg_pennes_check_finite(cg_pennes* h, int* finite);
 int cg_pennes_get_state(cg_pennes* h, float* theta, float* theta_max, float* dose);
+
+/* ------------------------------------------ post-processing on the device */
+
+/* Focal metrics of one record region (report/metrics.py:192-313): the
+ * fundamental's amplitude maximum over an interior box (first in C order,
+ * as argmax_interior, metrics.py:123-127), the -6 dB crossings of the
+ * profiles through it (extent_6db, metrics.py:140-152), the interior voxel
+ * count at or above half the peak (the -6 dB volume, metrics.py:228), and
+ * the values the reference reads at the peak. Amplitudes are the correctly
+ * rounded float32 |P|. */
+typedef struct cg_focus_input {
+  const float* p1;    /* device complex64 [nx][ny][nz]: harmonic 1 over the record region */
+  const float* p2;    /* device complex64 harmonic 2, or NULL */
+  const float* pmax;  /* device float32 time-domain max |p|, or NULL */
+  int shape[3];       /* record region extents */
+  int lo[3], hi[3];   /* interior box, record frame, half-open (interior_slices, metrics.py:96-120) */
+  int probe[3];       /* record-frame voxel whose |P1| is returned (the requested focus); any < 0: none */
+  int offset[3];      /* record origin minus the apex voxel: coordinate of index i is (i + offset) dx */
+  double dx;          /* voxel size [m] */
+} cg_focus_input;
+
+typedef struct cg_focus_report {
+  long long peak;          /* record-frame linear index of the interior |P1| maximum */
+  float p_peak;            /* |P1| there */
+  float p_max_at_peak;     /* p_max there (NaN without p_max) */
+  long long n_above_half;  /* interior voxels with |P1| >= 0.5 p_peak */
+  float p_probe;           /* |P1| at the probe voxel (NaN without one) */
+  int has_a2;              /* 1 when harmonic 2 was given */
+  float a2_at_peak;        /* |P2| at the |P1| peak */
+  float a2_peak;           /* interior |P2| maximum */
+  long long a2_peak_index; /* its record-frame linear index (-1 without P2) */
+  int truncated[3];        /* x, y, z: the profile never falls below half the peak on one side */
+  double left[3], right[3];/* x, y, z -6 dB crossings [m] from the apex (NaN when truncated) */
+} cg_focus_report;
+
+/* On caller device buffers; queued on `stream` (a cudaStream_t) and
+ * synchronised before return. Allocates its few-KB scratch stream-ordered. */
+int cg_focus_metrics(const cg_focus_input* in, cg_focus_report* out, void* stream);
+/* On member `member`'s phasors of the last cg_solver_finalize (the solver
+ * fills p1, p2, pmax and shape itself; no host copy of the field). */
+int cg_solver_focus_metrics(cg_solver* s, int member, const cg_focus_input* in, cg_focus_report* out);
+
+/* Volumetric heating Q [W/m^3] from recorded phasors
+ * (HeatingSource.from_phasors, sensors.py:193-295):
+ *   Q = sum over terms t of (alpha_t |P_t|^2) / (rho c)
+ * in float64 in the given term order, rounded to float32, times `scale`
+ * in float32. The heating grid gets Q over the record region and 0 elsewhere.
+ * Label mode (n_labels > 0): coef[l][t] = alpha_t of material l and
+ * coef[l][n_terms] = 1 / (rho c) of l, float64, host memory; dense mode:
+ * float32 device maps with alpha_t = alpha * alpha_factor[t]. */
+typedef struct cg_heating_spec {
+  int n_terms;
+  int harmonics[8];          /* harmonic of each term (cg_solver_heating_q) */
+  const float* phasor[8];    /* device complex64 phasor of each term over the record region */
+  int shape[3];              /* record region extents */
+  int n_labels;              /* 0: dense mode */
+  const double* coef;        /* label mode: [n_labels][n_terms + 1], host */
+  const uint8_t* labels;     /* label mode: device label map */
+  const float* alpha;        /* dense mode: device maps */
+  const float* rho;
+  const float* c;
+  double alpha_factor[8];    /* dense mode: per-term multiplier of alpha (n^y) */
+  int map_shape[3];          /* extents of the label / dense maps */
+  int map_origin[3];         /* map voxel of record voxel (0, 0, 0) */
+  int q_shape[3];            /* heating grid */
+  int q_origin[3];           /* heating-grid voxel of record voxel (0, 0, 0) */
+  float scale;
+} cg_heating_spec;
+
+/* Q into the caller's device buffer q_dev [q_shape]; queued on `stream`,
+ * synchronised before return. term_sums (host, n_terms, or NULL) receives
+ * each term's float64 sum over the record region (its mean times the voxel
+ * count: the reference's mean_q_by_harmonic_w_m3, sensors.py:272). */
+int cg_heating_q(const cg_heating_spec* spec, float* q_dev, double* term_sums, void* stream);
+/* The same from member `member`'s phasors of the last cg_solver_finalize:
+ * the solver fills phasor[] from harmonics[] and shape; in label mode with
+ * labels == NULL it uses its own label map (padded frame, map_origin = the
+ * record box start). The field stays on the device: q_dev can go straight
+ * to cg_pennes_set_coefficients / cg_pennes_set_labels as their q. */
+int cg_solver_heating_q(cg_solver* s, int member, const cg_heating_spec* spec, float* q_dev,
+                        double* term_sums);
+
+/* Plain device buffers for callers without a CUDA runtime of their own. */
+int cg_buffer_alloc(size_t bytes, void** out);
+int cg_buffer_free(void* p);
+/* cudaMemcpy with the kind inferred from the pointers (host or device). */
+int cg_buffer_copy(void* dst, const void* src, size_t bytes);
 
 #ifdef __cplusplus
 }

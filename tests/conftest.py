@@ -79,3 +79,29 @@ PENNES_GOLDEN = ["pennes3d_insulated", "pennes2d_dirichlet_substep"]
 @pytest.fixture
 def golden():
     return load_golden
+
+
+FOCUS_GOLDEN = ["focus_h2_target", "focus_truncated"]
+
+
+def focus_case(name: str):
+    """A committed focal-metrics fixture as (SolverResult mirror, frame kwargs, medium or None, golden dict)."""
+    from types import SimpleNamespace
+
+    from caustica_gb300.contract import SolverResult
+
+    g = load_golden(name)
+    org = tuple(int(v) for v in g["origin"])
+    p1 = g["p1"]
+    phasors = {1: p1}
+    if "p2" in g:
+        phasors[2] = g["p2"]
+    region = tuple(slice(o, o + n) for o, n in zip(org, p1.shape))
+    res = SolverResult(phasor=p1, p_max=g["pmax"], region=region, dt=2.5e-8, spp=40, steps_total=1200,
+                       t_end_s=3.0e-5, tof_periods=12, converged_period=26, settle_capped=False,
+                       convergence_history=[], phasors=phasors, meta={"solver": "westervelt"})
+    focus = tuple(int(v) for v in g["focus"])
+    frame = dict(dx=float(g["dx"]), grid_shape=tuple(int(v) for v in g["grid_shape"]), pml_vox=int(g["pml_vox"]),
+                 apex_vox=tuple(int(v) for v in g["apex"]), focus_vox=None if focus[0] < 0 else focus)
+    med = SimpleNamespace(rho=g["rho"], c=g["c"]) if "rho" in g else None
+    return res, frame, med, json.loads(g["metrics"])

@@ -152,6 +152,81 @@ def bowl_source_case():
     print(f"bowl: {src.n_points} voxels")
 
 
+def _focal_field(shape, centre, widths, peak, seed, noise):
+    rng = np.random.default_rng(seed)
+    ax = np.meshgrid(*[np.arange(n, dtype=np.float64) for n in shape], indexing="ij")
+    r2 = sum(((a - c0) / w) ** 2 for a, c0, w in zip(ax, centre, widths))
+    ph = rng.uniform(-np.pi, np.pi)
+    f = peak * np.exp(-0.5 * r2) * np.exp(1j * (ph + 0.3 * ax[2]))
+    f = f + noise * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    return f.astype(np.complex64)
+
+
+def focus_case(name, *, grid_shape, pml_vox, region, centre, widths, apex, focus, harmonic2, dx, seed,
+               spike=None, a2_edge=None, medium=True):
+    """``report.metrics.focus_metrics`` on a synthetic focal field (metrics.py:192-313)."""
+    from caustica.report.metrics import FieldFrame, focus_metrics
+    from caustica.solvers.base import SolverResult
+
+    shape = tuple(len(range(*sl.indices(n))) for sl, n in zip(region, grid_shape))
+    org = tuple(sl.indices(n)[0] for sl, n in zip(region, grid_shape))
+    ctr = tuple(c0 - o for c0, o in zip(centre, org))
+    p1 = _focal_field(shape, ctr, widths, 1.2e6, seed, 2e3)
+    if spike is not None:  # a larger value inside the PML margin: must not win the argmax
+        p1[spike] = np.complex64(4e6)
+    phasors = {1: p1}
+    if harmonic2:
+        p2 = (0.08 * np.abs(p1).astype(np.float64) ** 2 / 1.2e6).astype(np.complex64) * np.complex64(1j)
+        if a2_edge is not None:  # a residue against the absorber
+            p2[a2_edge] = np.complex64(2.5e5)
+        phasors[2] = p2
+    rng = np.random.default_rng(seed + 1)
+    pmax = (np.abs(p1) * rng.uniform(1.0, 1.2, shape)).astype(np.float32)
+    res = SolverResult(phasor=p1, p_max=pmax, region=tuple(slice(o, o + n) for o, n in zip(org, shape)),
+                       dt=2.5e-8, spp=40, steps_total=1200, t_end_s=3.0e-5, tof_periods=12,
+                       converged_period=26, settle_capped=False, convergence_history=[],
+                       phasors=phasors, meta={"solver": "westervelt"})
+    frame = FieldFrame(dx=dx, grid_shape=grid_shape, pml_vox=pml_vox, apex_vox=apex, focus_vox=focus)
+    med = None
+    if medium:
+        mrng = np.random.default_rng(seed + 2)
+        lab = mrng.integers(0, 3, grid_shape)
+        med = types.SimpleNamespace(rho=np.array([1000.0, 1050.0, 1090.0], np.float32)[lab],
+                                    c=np.array([1500.0, 1560.0, 1610.0], np.float32)[lab])
+    m = focus_metrics(res, frame, source_amplitude=1e5, medium=med)
+    out = {"p1": p1, "pmax": pmax, "origin": np.array(org), "grid_shape": np.array(grid_shape),
+           "pml_vox": np.int64(pml_vox), "apex": np.array(apex), "dx": np.float64(dx),
+           "focus": np.array(focus if focus is not None else (-1, -1, -1)),
+           "metrics": np.array(json.dumps(m))}
+    if harmonic2:
+        out["p2"] = phasors[2]
+    if med is not None:
+        out["rho"], out["c"] = med.rho, med.c
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(f"{name}: peak {m['peak']['p_pa']} at {m['peak']['voxel_grid']}, warnings {len(m['warnings'])}")
+
+
+def heating_case(name, *, shape, seed, harmonics, y):
+    """``HeatingSource.from_phasors`` on label-valued maps (sensors.py:193-295)."""
+    from caustica.sensors import HeatingSource
+
+    rng = np.random.default_rng(seed)
+    labels = rng.integers(0, 4, shape).astype(np.uint8)
+    table = np.array([[0.0, 1000.0, 1500.0], [4.3, 1050.0, 1560.0], [12.5, 1090.0, 1610.0],
+                      [55.0, 1900.0, 2800.0]], np.float32)  # alpha_f0 [Np/m], rho, c
+    alpha, rho, c = (table[labels, i] for i in range(3))
+    phasors = {n: (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+               * np.complex64(1e6 / n) for n in harmonics}
+    hs = HeatingSource.from_phasors(phasors, alpha=alpha, rho=rho, c=c, dx=0.3e-3,
+                                    harmonics=harmonics, alpha_power_law_y=y)
+    out = {"labels": labels, "table": table, "harmonics": np.array(harmonics), "y": np.float64(y),
+           "q": hs.q}
+    for n, p in phasors.items():
+        out[f"p{n}"] = p
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(f"{name}: q max {float(hs.q.max()):.4g}")
+
+
 def main(src_path: str) -> None:
     sys.path.insert(0, src_path)
     import caustica.core.backend as cb
@@ -184,6 +259,14 @@ def main(src_path: str) -> None:
     pennes_case("pennes2d_dirichlet_substep", shape=(12, 10), dx=0.25e-3, seed=71, dt=0.2, n_steps=12,
                 boundary="dirichlet", on_unstable="substep", reference_temperature_c=36.0)
     bowl_source_case()
+    focus_case("focus_h2_target", grid_shape=(40, 36, 48), pml_vox=4,
+               region=(slice(2, 38), slice(1, 35), slice(3, 46)), centre=(21, 17, 28), widths=(2.5, 3.0, 7.0),
+               apex=(20, 18, 5), focus=(22, 17, 27), harmonic2=True, dx=0.25e-3, seed=81,
+               spike=(1, 10, 20), a2_edge=(31, 12, 30))
+    focus_case("focus_truncated", grid_shape=(32, 30, 40), pml_vox=3,
+               region=(slice(0, 32), slice(0, 30), slice(0, 40)), centre=(15, 14, 20), widths=(2.0, 40.0, 5.0),
+               apex=(16, 15, 0), focus=None, harmonic2=False, dx=0.3e-3, seed=91, medium=False)
+    heating_case("heating_q_h12", shape=(14, 12, 18), seed=101, harmonics=(1, 2), y=1.1)
 
 
 if __name__ == "__main__":

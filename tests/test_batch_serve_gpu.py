@@ -27,6 +27,22 @@ def _setup(shape, seed, nonlinear=False, n_src=20):
     return grid, med, idx, rng
 
 
+def _same_metrics(a, b, where):
+    """Equal structure and integers; floats within the rounding the metrics are reported with."""
+    if isinstance(a, dict):
+        assert isinstance(b, dict) and a.keys() == b.keys(), where
+        for k in a:
+            _same_metrics(a[k], b[k], where + (k,))
+    elif isinstance(a, list):
+        assert isinstance(b, list) and len(a) == len(b), where
+        for x, y in zip(a, b):
+            _same_metrics(x, y, where)
+    elif isinstance(a, float) and isinstance(b, float):
+        assert a == pytest.approx(b, rel=1e-5, abs=0.2), where
+    else:
+        assert a == b, where
+
+
 def _solo(grid, med, idx, ph, spec, nonlinear, harmonics=(1,)):
     src = cg.CWSource(indices=idx, phases=ph, amplitude=2e5, f0=1e6)
     s = cg.WesterveltKSpaceGB300() if nonlinear else cg.LinearKSpaceGB300()
@@ -67,13 +83,17 @@ def test_server_results_are_the_same_alone_and_in_the_mix():
         reqs.append(serve.Request(grid=grid_a, medium=med_a, source=src, spec=spec, tag=("a", k)))
     grid_b, med_b, idx_b, rng_b = _setup((24, 16, 24), 4, nonlinear=True)
     src_b = cg.CWSource(indices=idx_b, phases=np.zeros(len(idx_b), np.float32), amplitude=2e5, f0=1e6)
+    frame_b = cg.FieldFrame(dx=grid_b.dx, grid_shape=grid_b.shape, pml_vox=grid_b.pml_vox, apex_vox=(12, 8, 2),
+                            focus_vox=(12, 8, 14))
     reqs.append(serve.Request(grid=grid_b, medium=med_b, source=src_b, spec=spec, nonlinear=True, harmonics=(1, 2),
-                              tag=("b", 0)))
+                              frame=frame_b, tag=("b", 0)))
     tm = cg.ThermalMedium.homogeneous(grid_a.shape, k=0.5, rho=1000.0, specific_heat=3600.0, perfusion=5e-4,
                                       dx=grid_a.dx)
     src_t = cg.CWSource(indices=idx_a, phases=np.zeros(len(idx_a), np.float32), amplitude=2e5, f0=1e6)
     reqs.append(serve.Request(grid=grid_a, medium=med_a, source=src_t, spec=spec, tag=("t", 0),
-                              thermal={"medium": tm, "dt": 0.05, "n_heat": 20, "n_cool": 10, "q_scale": 1e4}))
+                              thermal={"medium": tm, "dt": 0.05, "n_heat": 20, "n_cool": 10, "q_scale": 1e4},
+                              frame=cg.FieldFrame(dx=grid_a.dx, grid_shape=grid_a.shape, pml_vox=grid_a.pml_vox,
+                                                  apex_vox=(8, 12, 2))))
     with serve.Server(max_pack=8) as srv:
         futs = [srv.submit(r) for r in reqs]
         outs = [f.result(timeout=300) for f in futs]
@@ -84,6 +104,13 @@ def test_server_results_are_the_same_alone_and_in_the_mix():
         solo = _solo(r.grid, r.medium, r.source.indices, r.source.phases, r.spec, r.nonlinear, r.harmonics)
         for h in r.harmonics:
             assert rel_l2(o.result.phasors[h], solo.phasors[h]) < 1e-6, r.tag
+        if r.frame is not None:
+            # device metrics of the packed handle == metrics of the solo result
+            want_m = cg.focus_metrics(solo, r.frame, source_amplitude=r.source.amplitude, medium=r.medium)
+            for k in ("peak", "focal_spot", "harmonics", "target"):
+                _same_metrics(o.metrics.get(k), want_m.get(k), (r.tag, k))
+        else:
+            assert o.metrics is None
         if r.thermal is not None:
             want = serve.run_thermal(r, solo)
             assert np.abs(o.thermal.temperature - want.temperature).max() < 1e-5
