@@ -283,4 +283,13 @@ __device__ __forceinline__ void fft2(const float2 (&v_in)[A], float2 (&w)[B], in
   __syncthreads();
 }
 
+// Asynchronous 16-byte global -> shared copy (L2 only), completed by
+// cp_async_wait0 and made visible to the block by a following barrier.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 }  // namespace cgf

@@ -30,8 +30,12 @@ using cgf::Split;
 using cgf::fft2;
 using cgf::static_for;
 
-template <int N>
-__global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(int mode, Dims d, Tables t, float2* __restrict__ S0,
+// One instantiation per mode keeps each kernel's code small enough for the
+// instruction cache (the x-pass gradient loops over one copy of its inverse
+// transform; the y-pass modes stay straight-line, where the compiler hoists
+// the next input's loads above the current transform).
+template <int N, int MODE>
+__global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(Dims d, Tables t, float2* __restrict__ S0,
                                                          float2* __restrict__ S1, float2* __restrict__ S2) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
   using Ex = RowEx<A, B>;
@@ -58,14 +62,12 @@ __global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(int mode,
       dst[off + s + A * b] = w[b];
     });
   };
-  if (mode == Y_FWD || mode == Y_INV) {
+  if constexpr (MODE == Y_FWD || MODE == Y_INV) {
     load(S0);
-    if (mode == Y_FWD) fft2<A, B, false>(v, w, s, tw, ex);
-    else fft2<A, B, true>(v, w, s, tw, ex);
+    fft2<A, B, MODE == Y_INV>(v, w, s, tw, ex);
     store(S0);
-    return;
-  }
-  if (mode == Y_INV_GRAD) {
+  } else if constexpr (MODE == Y_INV_GRAD) {
+    // S1 <- IFFT(S1); S0 <- IFFT(i ky S2); S2 <- IFFT(S2)
     load(S1);
     fft2<A, B, true>(v, w, s, tw, ex);
     store(S1);
@@ -80,28 +82,28 @@ __global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(int mode,
     store(S0);
     fft2<A, B, true>(v, w, s, tw, ex);
     store(S2);
-    return;
+  } else {
+    // Y_FWD_DIV: S1 <- FFT(S1); S0 <- i ky FFT(S0) + FFT(S2)
+    load(S1);
+    fft2<A, B, false>(v, w, s, tw, ex);
+    store(S1);
+    load(S0);
+    fft2<A, B, false>(v, w, s, tw, ex);
+    float2 h[B];
+    static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const float k = (s < A) ? t.ky[s + A * b] : 0.f;
+      h[b] = c_muli(c_scale(w[b], k));
+    });
+    load(S2);
+    fft2<A, B, false>(v, w, s, tw, ex);
+    static_for<0, B>([&](auto bi) { w[decltype(bi)::value] = c_add(w[decltype(bi)::value], h[decltype(bi)::value]); });
+    store(S0);
   }
-  // Y_FWD_DIV: S1 = FFT(S1); S0 = i ky FFT(S0) + FFT(S2)
-  load(S1);
-  fft2<A, B, false>(v, w, s, tw, ex);
-  store(S1);
-  load(S0);
-  fft2<A, B, false>(v, w, s, tw, ex);
-  float2 h[B];
-  static_for<0, B>([&](auto bi) {
-    constexpr int b = decltype(bi)::value;
-    const float k = (s < A) ? t.ky[s + A * b] : 0.f;
-    h[b] = c_muli(c_scale(w[b], k));
-  });
-  load(S2);
-  fft2<A, B, false>(v, w, s, tw, ex);
-  static_for<0, B>([&](auto bi) { w[decltype(bi)::value] = c_add(w[decltype(bi)::value], h[decltype(bi)::value]); });
-  store(S0);
 }
 
-template <int N>
-__global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(int mode, Dims d, Tables t, float kcoef, float invN,
+template <int N, int MODE>
+__global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, Tables t, float kcoef, float invN,
                                                          float2* __restrict__ S0, float2* __restrict__ S1,
                                                          float2* __restrict__ S2) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
@@ -140,49 +142,51 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(int mode,
     });
   };
   auto kappa = [&](int k) { return sinc_a2(kcoef * (t.kx2[k] + kyz2)) * invN; };
-  if (mode == X_FWD || mode == X_INV) {
+  if constexpr (MODE == X_FWD || MODE == X_INV) {
     load(S0);
-    if (mode == X_FWD) fft2<A, B, false>(v, w, s, tw, exf);
-    else fft2<A, B, true>(v, w, s, tw, exf);
+    fft2<A, B, MODE == X_INV>(v, w, s, tw, exf);
     if (valid && s < A) static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       S0[base + (long long)(s + A * b) * ncol] = w[b];
     });
-    return;
-  }
-  if (mode == X_GRAD) {
+  } else if constexpr (MODE == X_GRAD) {
+    // S2 <- IFFT(kappa/N FFT(S0)); S1 <- IFFT(i kx kappa/N FFT(S0))
     load(S0);
     fft2<A, B, false>(v, w, s, tw, exf);
-    float2 g[B];
     static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int k = (s < A) ? s + A * b : 0;
-      const float2 q = c_scale(w[b], kappa(k));
-      w[b] = q;
-      g[b] = c_muli(c_scale(q, t.kx[k]));
+      w[b] = c_scale(w[b], kappa(k));
+    });
+#pragma unroll 1
+    for (int o = 0; o < 2; ++o) {
+      if (o == 1) static_for<0, B>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        const int k = (s < A) ? s + A * b : 0;
+        w[b] = c_muli(c_scale(w[b], t.kx[k]));
+      });
+      fft2<B, A, true>(w, z, s, twi, exi);
+      store_z(o == 0 ? S2 : S1);
+    }
+  } else {
+    // X_DIV: S0 <- IFFT(kappa/N (FFT(S0) + i kx FFT(S1)))
+    load(S1);
+    fft2<A, B, false>(v, w, s, tw, exf);
+    float2 h[B];
+    static_for<0, B>([&](auto bi) { h[decltype(bi)::value] = w[decltype(bi)::value]; });
+    load(S0);
+    fft2<A, B, false>(v, w, s, tw, exf);
+    static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const int k = (s < A) ? s + A * b : 0;
+      w[b] = c_scale(c_add(w[b], c_muli(c_scale(h[b], t.kx[k]))), kappa(k));
     });
     fft2<B, A, true>(w, z, s, twi, exi);
-    store_z(S2);
-    fft2<B, A, true>(g, z, s, twi, exi);
-    store_z(S1);
-    return;
+    store_z(S0);
   }
-  // X_DIV: S0 = IFFT(kappa/N (FFT(S0) + i kx FFT(S1)))
-  load(S1);
-  fft2<A, B, false>(v, w, s, tw, exf);
-  float2 h[B];
-  static_for<0, B>([&](auto bi) { h[decltype(bi)::value] = w[decltype(bi)::value]; });
-  load(S0);
-  fft2<A, B, false>(v, w, s, tw, exf);
-  static_for<0, B>([&](auto bi) {
-    constexpr int b = decltype(bi)::value;
-    const int k = (s < A) ? s + A * b : 0;
-    w[b] = c_scale(c_add(w[b], c_muli(c_scale(h[b], t.kx[k]))), kappa(k));
-  });
-  fft2<B, A, true>(w, z, s, twi, exi);
-  store_z(S0);
 }
 
+// twiddles | exchange
 template <int N>
 static size_t smem_y() {
   return sizeof(float2) * (N + CG_YP * RowEx<Split<N>::A, Split<N>::B>::SLAB);
@@ -196,9 +200,14 @@ bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1
                 cudaStream_t st) {
   const dim3 grid((unsigned)((d.nx * (long long)d.nzh + CG_YP - 1) / CG_YP), batch);
   switch (d.ny) {
-#define CASE(n)                                                                   \
-  case n:                                                                         \
-    kf_ypass<n><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(mode, d, t, S0, S1, S2); \
+#define CASE(n)                                                                                            \
+  case n:                                                                                                  \
+    switch (mode) {                                                                                        \
+      case Y_FWD: kf_ypass<n, Y_FWD><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break;       \
+      case Y_INV: kf_ypass<n, Y_INV><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break;       \
+      case Y_INV_GRAD: kf_ypass<n, Y_INV_GRAD><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break; \
+      default: kf_ypass<n, Y_FWD_DIV><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break;      \
+    }                                                                                                      \
     return true;
     CG_FAST_SIZES(CASE)
 #undef CASE
@@ -211,24 +220,36 @@ bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float inv
                 float2* S2, int batch, cudaStream_t st) {
   const dim3 grid((unsigned)(((long long)d.nzh * d.ny + CG_XP - 1) / CG_XP), batch);
   switch (d.nx) {
-#define CASE(n)                                                                                    \
-  case n:                                                                                          \
-    kf_xpass<n><<<grid, 16 * CG_XP, smem_x<n>(), st>>>(mode, d, t, kcoef, invN, S0, S1, S2); \
+#define XL(n, M) kf_xpass<n, M><<<grid, 16 * CG_XP, smem_x<n>(), st>>>(d, t, kcoef, invN, S0, S1, S2)
+#define CASE(n)                          \
+  case n:                                \
+    switch (mode) {                      \
+      case X_GRAD: XL(n, X_GRAD); break; \
+      case X_DIV: XL(n, X_DIV); break;   \
+      case X_FWD: XL(n, X_FWD); break;   \
+      default: XL(n, X_INV); break;      \
+    }                                    \
     return true;
     CG_FAST_SIZES(CASE)
 #undef CASE
+#undef XL
     default:
       return false;
   }
 }
 
+template <int N, int M>
+static int allow_yx() {
+  const int sy = (int)smem_y<N>(), sx = (int)smem_x<N>();
+  if (cudaFuncSetAttribute(kf_ypass<N, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, sy) != cudaSuccess) return -1;
+  if (cudaFuncSetAttribute(kf_xpass<N, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx) != cudaSuccess) return -1;
+  return 0;
+}
+
 int fast_prepare_yx() {
-#define SET(n)                                                                                      \
-  if (cudaFuncSetAttribute(kf_ypass<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<n>()) != \
-          cudaSuccess ||                                                                            \
-      cudaFuncSetAttribute(kf_xpass<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<n>()) != \
-          cudaSuccess)                                                                              \
-    return -1;
+  // Y_* and X_* modes are both 0..3
+#define SET(n)                                                                                        \
+  if (allow_yx<n, 0>() || allow_yx<n, 1>() || allow_yx<n, 2>() || allow_yx<n, 3>()) return -1;
   CG_FAST_SIZES(SET)
 #undef SET
   return 0;

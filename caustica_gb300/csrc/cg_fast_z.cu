@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_u(Dims d, T
   const bool lab = z_stage_labels<N>(lab_s, tab_s, m, d, x, y0);
   const uint8_t* la = lab_s + (2 * p) * N;
   const uint8_t* lb = la + N;
+#pragma unroll 1
   for (int comp = 0; comp < 3; ++comp) {
     float2* S = (comp == 0 ? S1 : (comp == 1 ? S0 : S2)) + off;
     const float* mk = (comp == 2) ? t.kz : nullptr;
@@ -243,9 +244,9 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_u(Dims d, T
   }
 }
 
-// mode 0: forward transform of p only; 2: inverse only into p; 1: full update
-template <int N>
-__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(int mode, Dims d, Tables t, MediumDev m, SourceDev src,
+// MODE 0: forward transform of p only; 2: inverse only into p; 1: full update
+template <int N, int MODE>
+__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(Dims d, Tables t, MediumDev m, SourceDev src,
                                                            RecordDev rec, const long long* ctl, int n_local,
                                                            int record, float* __restrict__ p_all,
                                                            float2* __restrict__ S0) {
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(int mode,
   const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
   __syncthreads();
   float2 w[B];
-  if (mode == 0) {
+  if constexpr (MODE == 0) {
     if (s < A) static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(int mode,
   } else {
     float4* tab_s = reinterpret_cast<float4*>(sm + Z::OFF_TAB);
     uint8_t* lab_s = reinterpret_cast<uint8_t*>(tab_s + 256);
-    const bool lab = (mode == 1) && z_stage_labels<N>(lab_s, tab_s, m, d, x, y0);
+    const bool lab = (MODE == 1) && z_stage_labels<N>(lab_s, tab_s, m, d, x, y0);
     const uint8_t* la = lab_s + (2 * p) * N;
     const uint8_t* lb = la + N;
     z_stage<N>(stg4, S, d, x, y0, nullptr);
@@ -292,14 +293,14 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(int mode,
     static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
-      pa[b] = (mode == 1 && s < A && va) ? __ldg(pb + rowa + n) : 0.f;
-      pbv[b] = (mode == 1 && s < A && vb) ? __ldg(pb + rowb + n) : 0.f;
+      pa[b] = (MODE == 1 && s < A && va) ? __ldg(pb + rowa + n) : 0.f;
+      pbv[b] = (MODE == 1 && s < A && vb) ? __ldg(pb + rowb + n) : 0.f;
     });
     __syncthreads();
     float2 v[A];
     z_inputs<N>(v, stg4, p, s);
     fft2<A, B, true>(v, w, s, tw, exi);
-    if (mode == 2) {
+    if constexpr (MODE == 2) {
       if (s < A) static_for<0, B>([&](auto bi) {
         constexpr int b = decltype(bi)::value;
         const int n = s + A * b;
@@ -395,14 +396,373 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(int mode,
       if (per < rec.max_periods) atomicMax(&rec.peaks[(long long)b_idx * rec.max_periods + per], s_peak);
     }
   }
-  float2 X[A];
-  fft2<B, A, false>(w, X, s, twf, exf);
-  z_split_store<N>(xb, X, S, d, x, y0, p, s, nullptr);
+  if constexpr (MODE != 2) {
+    float2 X[A];
+    fft2<B, A, false>(w, X, s, twf, exf);
+    z_split_store<N>(xb, X, S, d, x, y0, p, s, nullptr);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent, pipelined z-passes (ny a multiple of the tile height). Each CTA
+// walks a contiguous run of tiles -- for the u-pass all three velocity
+// components of a tile in turn, so the tile's labels load once -- and the half
+// spectrum of the next (tile, component) streams into shared memory with
+// cp.async while the current one is transformed. An item's staging buffer is
+// then reused as its exchange and split-store buffer, so the two buffers cost
+// what the single-item kernel's staging plus exchange cost and two CTAs still
+// fit on an SM.
+template <int N>
+struct ZPShape {
+  static constexpr int A = Split<N>::A, B = Split<N>::B, NH = N / 2 + 1;
+  static constexpr int EX_I = RowEx<A, B>::SLAB, EX_F = RowEx<B, A>::SLAB;
+  static constexpr int EX = EX_I > EX_F ? EX_I : EX_F;
+  static constexpr int B_STG = NH * 34, B_EX = CG_TILE * EX, B_XB = N * 17;  // float2 units
+  static constexpr int B_MAX = B_STG > B_EX ? (B_STG > B_XB ? B_STG : B_XB) : (B_EX > B_XB ? B_EX : B_XB);
+  static constexpr int BUF = (B_MAX + 1) / 2 * 2;  // even: float4-aligned
+  static constexpr int KZF = (NH + 3) / 4 * 2;     // k_z table (floats), float2 units, even
+  // twiddles (two orders) | k_z | two item buffers | material table | two label tiles
+  static constexpr size_t OFF_KZ = 2 * N, OFF_BUF = OFF_KZ + KZF, OFF_TAB = OFF_BUF + 2 * (size_t)BUF;
+  static constexpr size_t OFF_LAB = OFF_TAB + 2 * 256;
+  static constexpr size_t smem = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
+};
+
+// The half spectrum of tile (x, y0) of S into stg4[k * 17 + p], asynchronously.
+template <int N>
+__device__ __forceinline__ void z_prefetch(float4* stg4, const float2* __restrict__ S, const Dims& d, int x, int y0) {
+  constexpr int NH = N / 2 + 1;
+  const float2* base = S + (long long)x * NH * d.ny + y0;
+  for (int idx = threadIdx.x; idx < NH * CG_TILE; idx += blockDim.x) {
+    const int k = idx >> 4, pp = idx & 15;
+    cgf::cp_async16(stg4 + k * 17 + pp, base + (long long)k * d.ny + 2 * pp);
+  }
+}
+
+// The tile's labels (CG_ZROWS rows of N bytes, contiguous), asynchronously.
+template <int N>
+__device__ __forceinline__ void z_prefetch_labels(uint8_t* lab_s, const uint8_t* __restrict__ labels, const Dims& d,
+                                                  int x, int y0) {
+  const uint8_t* src = labels + ((long long)x * d.ny + y0) * N;
+  for (int i = threadIdx.x; i < CG_ZROWS * N / 16; i += blockDim.x) cgf::cp_async16(lab_s + 16 * i, src + 16 * i);
+}
+
+// z_inputs on a raw staged tile: times i*mk[k] when mk is given, Im of the
+// self-paired bins dropped, then the Hermitian extension.
+template <int N>
+__device__ __forceinline__ void z_inputs_raw(float2 (&v)[Split<N>::A], const float4* stg4, int p, int s,
+                                             const float* mk) {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  static_for<0, A>([&](auto ai) {
+    constexpr int a = decltype(ai)::value;
+    const int n = s + B * a;
+    float2 z = make_float2(0.f, 0.f);
+    if (s < B) {
+      const bool hi = 2 * n > N;
+      const int k = hi ? N - n : n;
+      const float4 f = stg4[k * 17 + p];
+      float2 fa = make_float2(f.x, f.y), fb = make_float2(f.z, f.w);
+      if (mk) {
+        const float kk = mk[k];
+        fa = c_muli(c_scale(fa, kk));
+        fb = c_muli(c_scale(fb, kk));
+      }
+      if (k == 0 || 2 * k == N) {
+        fa.y = 0.f;
+        fb.y = 0.f;
+      }
+      z = hi ? make_float2(fa.x + fb.y, fb.x - fa.y)   // conj(A) + i conj(B)
+             : make_float2(fa.x - fb.y, fa.y + fb.x);  // A + i B
+    }
+    v[a] = z;
+  });
+}
+
+template <int N>
+__device__ __forceinline__ void zp_tables(float2* sm, const Tables& t, const MediumDev& m) {
+  using Z = ZPShape<N>;
+  cgf::fill_twt<Z::A, Z::B>(sm, t.twz);
+  cgf::fill_twt<Z::B, Z::A>(sm + N, t.twz);
+  float* kz_s = reinterpret_cast<float*>(sm + Z::OFF_KZ);
+  for (int i = threadIdx.x; i < Z::NH; i += blockDim.x) kz_s[i] = t.kz[i];
+  float4* tab_s = reinterpret_cast<float4*>(sm + Z::OFF_TAB);
+  if (m.labels)
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) tab_s[i] = m.ltab[i];
+}
+
+template <int N>
+__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, Tables t, MediumDev m,
+                                                                       float* __restrict__ u, float2* __restrict__ S0,
+                                                                       float2* __restrict__ S1, float2* __restrict__ S2,
+                                                                       int n_members, int tiles_per_cta) {
+  using Z = ZPShape<N>;
+  constexpr int A = Z::A, B = Z::B;
+  extern __shared__ float2 sm[];
+  const int ytiles = d.ny / CG_ZROWS;
+  const long long per_member = (long long)d.nx * ytiles;
+  const long long total = per_member * n_members;
+  const long long t0 = (long long)blockIdx.x * tiles_per_cta;
+  const long long t1 = min(total, t0 + tiles_per_cta);
+  if (t0 >= t1) return;  // the whole CTA, before any barrier
+  zp_tables<N>(sm, t, m);
+  const float* kz_s = reinterpret_cast<const float*>(sm + Z::OFF_KZ);
+  const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
+  uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
+  const bool lab = m.labels != nullptr;
+  const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
+  auto spec = [&](int comp, long long b) { return (comp == 0 ? S1 : (comp == 1 ? S0 : S2)) + b * d.nspec; };
+  auto prefetch = [&](long long tile, int comp, int j) {
+    const long long b = tile / per_member, r = tile - b * per_member;
+    const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
+    z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), spec(comp, b), d, x, y0);
+    if (comp == 0 && lab) z_prefetch_labels<N>(lab0 + ((tile - t0) & 1) * CG_ZROWS * N, m.labels, d, x, y0);
+    cgf::cp_async_commit();
+  };
+  prefetch(t0, 0, 0);
+  int j = 0;
+  for (long long tile = t0; tile < t1; ++tile) {
+    const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
+    const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
+    const int ya = y0 + 2 * p, yb = ya + 1;
+    const float spx = t.sx[x];
+    const float spa = spx * t.sy[ya], spb = spx * t.sy[yb];
+    const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
+    const uint8_t* la = lab0 + ((tile - t0) & 1) * CG_ZROWS * N + (2 * p) * N;
+    const uint8_t* lb = la + N;
+#pragma unroll 1
+    for (int comp = 0; comp < 3; ++comp, j ^= 1) {
+      float* uc = u + ((long long)comp * n_members + b_idx) * d.ncell;
+      // this thread's velocities load while the staged spectrum is transformed
+      float ua[B], ub[B];
+      static_for<0, B>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        const int n = s + A * b;
+        ua[b] = (s < A) ? __ldg(uc + rowa + n) : 0.f;
+        ub[b] = (s < A) ? __ldg(uc + rowb + n) : 0.f;
+      });
+      cgf::cp_async_wait0();
+      __syncthreads();
+      {
+        long long nt = tile;
+        int nc = comp + 1;
+        if (nc == 3) {
+          nc = 0;
+          ++nt;
+        }
+        if (nt < t1) prefetch(nt, nc, j ^ 1);
+      }
+      float2* bufj = sm + Z::OFF_BUF + (size_t)j * Z::BUF;
+      float2 v[A], w[B];
+      z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, comp == 2 ? kz_s : nullptr);
+      __syncthreads();  // the staging is read: the buffer becomes the exchange
+      const RowEx<A, B> exi{bufj + p * Z::EX};
+      const RowEx<B, A> exf{bufj + p * Z::EX};
+      fft2<A, B, true>(v, w, s, sm, exi);
+      // u <- (u - dt/rho g) * absorb * sponge   (engine.py:462-464)
+      if (s < A) static_for<0, B>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        const int n = s + A * b;
+        const float sz = t.sz[n];
+        const float4 ca = lab ? tab_s[la[n]] : cell_coef(m, rowa + n);
+        const float4 cb = lab ? tab_s[lb[n]] : cell_coef(m, rowb + n);
+        float una = ua[b] - ca.x * w[b].x;
+        una = una * ca.z;
+        una = una * (spa * sz);
+        float unb = ub[b] - cb.x * w[b].y;
+        unb = unb * cb.z;
+        unb = unb * (spb * sz);
+        uc[rowa + n] = una;
+        uc[rowb + n] = unb;
+        w[b] = make_float2(una, unb);
+      });
+      float2 X[A];
+      fft2<B, A, false>(w, X, s, sm + N, exf);
+      z_split_store<N>(bufj, X, spec(comp, b_idx), d, x, y0, p, s, comp == 2 ? t.kz : nullptr);
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, Tables t, MediumDev m,
+                                                                       SourceDev src, RecordDev rec,
+                                                                       const long long* ctl, int n_local, int record,
+                                                                       float* __restrict__ p_all,
+                                                                       float2* __restrict__ S0, int n_members,
+                                                                       int tiles_per_cta) {
+  using Z = ZPShape<N>;
+  constexpr int A = Z::A, B = Z::B;
+  extern __shared__ float2 sm[];
+  __shared__ unsigned int s_peak;
+  const int ytiles = d.ny / CG_ZROWS;
+  const long long per_member = (long long)d.nx * ytiles;
+  const long long total = per_member * n_members;
+  const long long t0 = (long long)blockIdx.x * tiles_per_cta;
+  const long long t1 = min(total, t0 + tiles_per_cta);
+  if (t0 >= t1) return;  // the whole CTA, before any barrier
+  zp_tables<N>(sm, t, m);
+  if (threadIdx.x == 0) s_peak = 0u;
+  const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
+  uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
+  const bool lab = m.labels != nullptr;
+  const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
+  auto prefetch = [&](long long tile, int j) {
+    const long long b = tile / per_member, r = tile - b * per_member;
+    const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
+    z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), S0 + b * d.nspec, d, x, y0);
+    if (lab) z_prefetch_labels<N>(lab0 + j * CG_ZROWS * N, m.labels, d, x, y0);
+    cgf::cp_async_commit();
+  };
+  prefetch(t0, 0);
+  const long long n_step = ctl[0] + n_local;
+  const int m_bin = (int)(n_step % rec.spp);
+  const long long Ry = rec.hi[1] - rec.lo[1], Rz = rec.hi[2] - rec.lo[2];
+  const bool drive_on = src.S > 0 && n_step < src.n_drive;
+  const float4 dr = drive_on ? src.drive[n_step] : make_float4(0.f, 0.f, 0.f, 0.f);
+  int j = 0;
+  for (long long tile = t0; tile < t1; ++tile, j ^= 1) {
+    const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
+    const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
+    const int ya = y0 + 2 * p, yb = ya + 1;
+    float* pb = p_all + b_idx * d.ncell;
+    float2* S = S0 + b_idx * d.nspec;
+    const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
+    // this thread's pressures load while the staged spectrum is transformed
+    float pa[B], pbv[B];
+    static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const int n = s + A * b;
+      pa[b] = (s < A) ? __ldg(pb + rowa + n) : 0.f;
+      pbv[b] = (s < A) ? __ldg(pb + rowb + n) : 0.f;
+    });
+    cgf::cp_async_wait0();
+    __syncthreads();
+    if (tile + 1 < t1) prefetch(tile + 1, j ^ 1);
+    float2* bufj = sm + Z::OFF_BUF + (size_t)j * Z::BUF;
+    const uint8_t* la = lab0 + j * CG_ZROWS * N + (2 * p) * N;
+    const uint8_t* lb = la + N;
+    float2 v[A], w[B];
+    z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, nullptr);
+    __syncthreads();  // the staging is read: the buffer becomes the exchange
+    const RowEx<A, B> exi{bufj + p * Z::EX};
+    const RowEx<B, A> exf{bufj + p * Z::EX};
+    fft2<A, B, true>(v, w, s, sm, exi);
+    const float spx = t.sx[x];
+    const float spa = spx * t.sy[ya], spb = spx * t.sy[yb];
+    // p <- (p - (rho c^2 dt [+ 2 beta dt p]) div u) * absorb * sponge   (engine.py:470-477)
+    if (s < A) static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const int n = s + A * b;
+      const float sz = t.sz[n];
+      const float4 ca = lab ? tab_s[la[n]] : cell_coef(m, rowa + n);
+      const float4 cb = lab ? tab_s[lb[n]] : cell_coef(m, rowb + n);
+      const float poa = pa[b], pob = pbv[b];
+      float pna = m.nonlinear ? poa - (ca.y + ca.w * poa) * w[b].x : poa - ca.y * w[b].x;
+      float pnb = m.nonlinear ? pob - (cb.y + cb.w * pob) * w[b].y : pob - cb.y * w[b].y;
+      pna = pna * ca.z;
+      pnb = pnb * cb.z;
+      w[b] = make_float2(pna * (spa * sz), pnb * (spb * sz));
+    });
+    // source (engine.py:478-482): entries of rows ya, yb owned by this thread
+    if (drive_on && s < A) {
+      const int ra = x * d.ny + ya;
+      const int e0 = src.row_ptr[ra], e1 = src.row_ptr[ra + 1], e2 = src.row_ptr[ra + 2];
+      for (int e = e0; e < e2; ++e) {
+        const int zz = src.zidx[e];
+        if (zz % A != s) continue;
+        const int k2 = zz / A;
+        const float acv = src.ac[b_idx * src.S + e];
+        const float asv = src.as[b_idx * src.S + e];
+        const float add = dr.x * (dr.y * acv - dr.z * asv);
+        const bool on_b = e >= e1;
+        static_for<0, B>([&](auto bi) {
+          constexpr int b = decltype(bi)::value;
+          if (k2 == b) {
+            if (on_b) w[b].y += add;
+            else w[b].x += add;
+          }
+        });
+      }
+    }
+    // write p, convergence peak, record window
+    unsigned int lpeak = 0u;
+    const bool x_conv = x >= rec.clo[0] && x < rec.chi[0];
+    const bool x_rec = record && x >= rec.lo[0] && x < rec.hi[0];
+    float* bins = rec.bins + (b_idx * rec.spp + m_bin) * rec.nrec;
+    float* comp = rec.comp + (b_idx * rec.spp + m_bin) * rec.nrec;
+    float* pmax = rec.pmax + b_idx * rec.nrec;
+    if (s < A) static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const int n = s + A * b;
+      for (int rr = 0; rr < 2; ++rr) {
+        const int y = rr ? yb : ya;
+        const float pn = rr ? w[b].y : w[b].x;
+        pb[(rr ? rowb : rowa) + n] = pn;
+        const float apn = fabsf(pn);
+        if (x_conv && y >= rec.clo[1] && y < rec.chi[1] && n >= rec.clo[2] && n < rec.chi[2])
+          lpeak = max(lpeak, __float_as_uint(apn));
+        if (x_rec && y >= rec.lo[1] && y < rec.hi[1] && n >= rec.lo[2] && n < rec.hi[2]) {
+          const long long ri = ((long long)(x - rec.lo[0]) * Ry + (y - rec.lo[1])) * Rz + (n - rec.lo[2]);
+          const float sv = bins[ri], cm0 = comp[ri];
+          const float yk = pn - cm0;
+          const float tk = sv + yk;
+          comp[ri] = (tk - sv) - yk;
+          bins[ri] = tk;
+          const float pm = pmax[ri];
+          pmax[ri] = (apn > pm || apn != apn) ? apn : pm;
+        }
+      }
+    });
+    lpeak = __reduce_max_sync(0xffffffffu, lpeak);
+    if ((threadIdx.x & 31) == 0 && lpeak) atomicMax(&s_peak, lpeak);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (s_peak != 0u) {
+        const long long per = n_step / rec.spp;
+        if (per < rec.max_periods) atomicMax(&rec.peaks[b_idx * rec.max_periods + per], s_peak);
+      }
+      s_peak = 0u;  // the next tile's updates follow the next item's barrier
+    }
+    float2 X[A];
+    fft2<B, A, false>(w, X, s, sm + N, exf);
+    z_split_store<N>(bufj, X, S, d, x, y0, p, s, nullptr);
+  }
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      n = 152;
+  }
+  return n;
+}
+
+// Persistent grid: about CG_FAST_MINB CTAs per SM, every CTA a run of equal length.
+static void persistent_grid(long long total, int* grid, int* per_cta) {
+  const long long slots = (long long)sm_count() * CG_FAST_MINB;
+  const long long g0 = total < slots ? total : slots;
+  const long long per = (total + g0 - 1) / g0;
+  *per_cta = (int)per;
+  *grid = (int)((total + per - 1) / per);
 }
 
 bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
                   int batch, cudaStream_t st) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
+  if (d.ny % CG_ZROWS == 0) {
+    int g = 0, per = 0;
+    persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, &g, &per);
+    switch (d.nz) {
+#define CASE(n)                                                                                          \
+  case n:                                                                                                \
+    kfp_zpass_u<n><<<g, CG_THREADS, ZPShape<n>::smem, st>>>(d, t, m, u, S0, S1, S2, batch, per);         \
+    return true;
+      CG_FAST_SIZES(CASE)
+#undef CASE
+      default:
+        return false;
+    }
+  }
   switch (d.nz) {
 #define CASE(n)                                                                       \
   case n:                                                                             \
@@ -419,14 +779,33 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
                   const RecordDev& rec, const long long* ctl, int n_local, int record, float* p, float2* S0,
                   int batch, cudaStream_t st) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
+  if (mode == 1 && d.ny % CG_ZROWS == 0) {
+    int g = 0, per = 0;
+    persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, &g, &per);
+    switch (d.nz) {
+#define CASE(n)                                                                                               \
+  case n:                                                                                                     \
+    kfp_zpass_p<n><<<g, CG_THREADS, ZPShape<n>::smem, st>>>(d, t, m, src, rec, ctl, n_local, record, p, S0, \
+                                                            batch, per);                                      \
+    return true;
+      CG_FAST_SIZES(CASE)
+#undef CASE
+      default:
+        return false;
+    }
+  }
   switch (d.nz) {
-#define CASE(n)                                                                                            \
-  case n:                                                                                                  \
-    kf_zpass_p<n><<<grid, CG_THREADS, ZShape<n>::smem, st>>>(mode, d, t, m, src, rec, ctl, n_local, record, \
-                                                              p, S0);                                      \
+#define ZL(n, M) \
+  kf_zpass_p<n, M><<<grid, CG_THREADS, ZShape<n>::smem, st>>>(d, t, m, src, rec, ctl, n_local, record, p, S0)
+#define CASE(n)                                         \
+  case n:                                               \
+    if (mode == 0) ZL(n, 0);                            \
+    else if (mode == 1) ZL(n, 1);                       \
+    else ZL(n, 2);                                      \
     return true;
     CG_FAST_SIZES(CASE)
 #undef CASE
+#undef ZL
     default:
       return false;
   }
@@ -436,7 +815,15 @@ int fast_prepare_z() {
 #define SET(n)                                                                                          \
   if (cudaFuncSetAttribute(kf_zpass_u<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
           cudaSuccess ||                                                                                \
-      cudaFuncSetAttribute(kf_zpass_p<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
+      cudaFuncSetAttribute(kf_zpass_p<n, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
+          cudaSuccess ||                                                                                \
+      cudaFuncSetAttribute(kf_zpass_p<n, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
+          cudaSuccess ||                                                                                \
+      cudaFuncSetAttribute(kf_zpass_p<n, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
+          cudaSuccess ||                                                                                \
+      cudaFuncSetAttribute(kfp_zpass_u<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZPShape<n>::smem) != \
+          cudaSuccess ||                                                                                \
+      cudaFuncSetAttribute(kfp_zpass_p<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZPShape<n>::smem) != \
           cudaSuccess)                                                                                  \
     return -1;
   CG_FAST_SIZES(SET)
