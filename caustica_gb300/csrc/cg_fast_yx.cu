@@ -9,9 +9,10 @@
 #include "cg_kspace.cuh"
 
 // resident CTAs per SM the register allocation targets (y: 8-row CTAs,
-// x: 16-column CTAs; both ~85 registers per thread)
+// ~102 registers per thread, no spills; x: 16-column CTAs, ~85 registers;
+// both measured best on a 192^2 x 256 grid)
 #ifndef CG_FAST_MINB_Y
-#define CG_FAST_MINB_Y 6
+#define CG_FAST_MINB_Y 5
 #endif
 #ifndef CG_FAST_MINB_X
 #define CG_FAST_MINB_X 3
