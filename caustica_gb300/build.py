@@ -23,7 +23,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libcaustica_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["cg_kspace.cu", "cg_pennes.cu", "cg_fast_yx.cu", "cg_fast_z.cu", "cg_post.cu"]
+SOURCES = ["cg_kspace.cu", "cg_pennes.cu", "cg_fast_yx.cu", "cg_fast_z.cu", "cg_post.cu", "cg_fused_xy.cu"]
 
 
 def nvcc() -> str:

@@ -811,6 +811,13 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
     solver_free(s);
     return CG_ERR_CUDA;
   }
+  {
+    // CG_FUSED_XY=1 selects the cluster-fused transverse passes where they
+    // apply; measured slower than the three-pass chain on a 192^2 x 256 grid
+    // (one CTA per SM, cluster placement leaves SMs idle), so opt-in
+    const char* env = getenv("CG_FUSED_XY");
+    s->fused_xy = (env && env[0] == '1') ? fused_xy_supported(s->d) : 0;
+  }
   rc = cg_solver_reset(s);
   if (rc != CG_OK) {
     solver_free(s);
@@ -985,26 +992,45 @@ static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = 
 #define EV(i) \
   if (ev) cudaEventRecord(ev[i], st)
   EV(0);
-  if (!fast_ypass(Y_FWD, d, t, s->S0, s->S1, s->S2, B, st))
-    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD, d, s->py, t, s->S0, s->S1, s->S2);
-  EV(1);
-  if (!fast_xpass(X_GRAD, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
-    k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_GRAD, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
-  EV(2);
-  if (!fast_ypass(Y_INV_GRAD, d, t, s->S0, s->S1, s->S2, B, st))
-    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
+  const bool fx = s->fused_xy != 0;
+  if (fx) {
+    if (!fused_xy(true, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st)) {
+      cg_set_error("fused transverse pass launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return CG_ERR_CUDA;
+    }
+    EV(1);
+    EV(2);
+  } else {
+    if (!fast_ypass(Y_FWD, d, t, s->S0, s->S1, s->S2, B, st))
+      k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD, d, s->py, t, s->S0, s->S1, s->S2);
+    EV(1);
+    if (!fast_xpass(X_GRAD, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
+      k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_GRAD, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
+    EV(2);
+    if (!fast_ypass(Y_INV_GRAD, d, t, s->S0, s->S1, s->S2, B, st))
+      k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
+  }
   EV(3);
   if (!fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st))
     k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
   EV(4);
-  if (!fast_ypass(Y_FWD_DIV, d, t, s->S0, s->S1, s->S2, B, st))
-    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD_DIV, d, s->py, t, s->S0, s->S1, s->S2);
-  EV(5);
-  if (!fast_xpass(X_DIV, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
-    k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_DIV, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
-  EV(6);
-  if (!fast_ypass(Y_INV, d, t, s->S0, s->S1, s->S2, B, st))
-    k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
+  if (fx) {
+    if (!fused_xy(false, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st)) {
+      cg_set_error("fused transverse pass launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return CG_ERR_CUDA;
+    }
+    EV(5);
+    EV(6);
+  } else {
+    if (!fast_ypass(Y_FWD_DIV, d, t, s->S0, s->S1, s->S2, B, st))
+      k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD_DIV, d, s->py, t, s->S0, s->S1, s->S2);
+    EV(5);
+    if (!fast_xpass(X_DIV, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
+      k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_DIV, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
+    EV(6);
+    if (!fast_ypass(Y_INV, d, t, s->S0, s->S1, s->S2, B, st))
+      k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
+  }
   EV(7);
   if (!fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st))
     k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
@@ -1168,7 +1194,7 @@ extern "C" int cg_solver_info(const cg_solver* s, long long* out /* 8 */) {
   out[4] = (long long)s->smem_x;
   out[5] = (long long)s->smem_z;
   out[6] = s->B;
-  out[7] = 8;  // kernel launches per step
+  out[7] = s->fused_xy ? 4 : 8;  // kernel launches per step
   return CG_OK;
 }
 

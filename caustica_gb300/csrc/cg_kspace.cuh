@@ -106,6 +106,10 @@ __device__ __forceinline__ float4 cell_coef(const MediumDev& m, long long i) {
 // (returns false otherwise; the caller then uses the generic kernel).
 bool fast_has(int n);
 int fast_prepare();  // lift the dynamic shared-memory limits (once per device)
+// fused transverse passes (cg_fused_xy.cu): 1 when they apply to the grid
+int fused_xy_supported(const Dims& d);
+bool fused_xy(bool grad, const Dims& d, const Tables& t, float kcoef, float invN, float2* S0, float2* S1,
+              float2* S2, int batch, cudaStream_t st);
 bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1, float2* S2, int batch,
                 cudaStream_t st);
 bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float invN, float2* S0, float2* S1,

@@ -38,6 +38,7 @@ struct cg_solver {
   int has_medium = 0;
   cudaStream_t stream = nullptr;
   size_t smem_y = 0, smem_x = 0, smem_z = 0;
+  int fused_xy = 0;  // the transverse passes run as two cluster launches per step
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one period, record off/on
   // phasors of the last finalize, [B][nh][nrec], kept for device post-processing
   float2* ph = nullptr;

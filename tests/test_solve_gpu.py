@@ -103,3 +103,17 @@ def test_bowl_focus_against_the_oracle_midsize():
     a, b = np.abs(res.phasor), np.abs(ref["phasor"])
     assert np.unravel_index(a.argmax(), a.shape) == np.unravel_index(b.argmax(), b.shape)
     assert abs(a.max() - b.max()) / b.max() < 1e-3
+    # focal metrics (device) against the same metrics of the FP64 field: peak within 0.1 %,
+    # -6 dB extents within one voxel
+    from oracle import metrics as om
+
+    frame = cg.FieldFrame(dx=dx, grid_shape=shape, pml_vox=4, apex_vox=(16, 16, 6))
+    m = cg.focus_metrics(res, frame)
+    m_ref = om.focus_metrics(ref["phasor"], origin=(0, 0, 0), grid_shape=shape, pml_vox=4, apex=(16, 16, 6),
+                             dx=dx, p_max=ref["p_max"], amp=np.abs(ref["phasor"]).astype(np.float32))
+    assert m["peak"]["voxel_grid"] == m_ref["peak"]["voxel_grid"]
+    assert abs(m["peak"]["p_pa"] - m_ref["peak"]["p_pa"]) / m_ref["peak"]["p_pa"] < 1e-3
+    for k in ("axial_6db", "lateral_x_6db", "lateral_y_6db"):
+        assert m["focal_spot"][k]["truncated"] == m_ref["focal_spot"][k]["truncated"]
+        if not m_ref["focal_spot"][k]["truncated"]:
+            assert abs(m["focal_spot"][k]["width_mm"] - m_ref["focal_spot"][k]["width_mm"]) <= dx * 1e3

@@ -14,7 +14,11 @@ pytestmark = pytest.mark.gpu
 CASES = [((12, 10, 16), False, True), ((9, 12, 10), True, True), ((16, 16, 24), True, False), ((1, 1, 40), False, True),
          ((1, 18, 20), True, True), ((48, 40, 64), True, True),
          # every axis on the size-specialised path
-         ((32, 32, 32), True, True), ((24, 48, 96), False, True), ((16, 64, 48), True, False)]
+         ((32, 32, 32), True, True), ((24, 48, 96), False, True), ((16, 64, 48), True, False),
+         # square transverse planes: the fused cluster passes
+         ((64, 64, 32), True, True), ((96, 96, 24), False, True), ((128, 128, 16), True, True),
+         ((160, 160, 16), True, False), ((192, 192, 16), True, True)]
+FUSED = {64, 96, 128, 160, 192}
 
 
 def _setup(shape, nonlinear, hetero, seed=0):
@@ -39,8 +43,10 @@ def _setup(shape, nonlinear, hetero, seed=0):
     return plan, grid, med, rng
 
 
+@pytest.mark.parametrize("fused", ["0", "1"])
 @pytest.mark.parametrize("shape,nonlinear,hetero", CASES)
-def test_steps_match_the_oracle_step(shape, nonlinear, hetero):
+def test_steps_match_the_oracle_step(shape, nonlinear, hetero, fused, monkeypatch):
+    monkeypatch.setenv("CG_FUSED_XY", fused)
     plan, grid, med, rng = _setup(shape, nonlinear, hetero)
     p0 = (rng.standard_normal(plan.padded) * 1e5).astype(np.float32)
     u0 = [(rng.standard_normal(plan.padded) * 0.05).astype(np.float32) for _ in range(plan.nd)]
@@ -53,6 +59,8 @@ def test_steps_match_the_oracle_step(shape, nonlinear, hetero):
         # the source ramp is exactly zero at t = 0, so step 0 injects nothing
         dev.run_steps(1)
         p1, u1 = dev.get_state()
+        on = fused == "1" and shape[0] == shape[1] and shape[0] in FUSED
+        assert dev.launches_per_step == (4 if on else 8)
     maps = ok.medium_maps(med.alpha, med.rho, med.c, med.beta, plan.padded, plan.dt, nonlinear, np.float64)
     ks = ok.k_vectors(plan.padded, plan.dx, np.float64)
     kap = ok.kappa_sinc(ks, plan.c_max, plan.dt, np.float64)
@@ -68,3 +76,23 @@ def test_steps_match_the_oracle_step(shape, nonlinear, hetero):
         gu = u1[3 - plan.nd + i, 0].reshape(plan.padded)
         assert np.abs(gu - ur[i]).max() / np.abs(ur[i]).max() < 2e-6
     del nsteps
+
+
+@pytest.mark.parametrize("shape,nonlinear", [((96, 96, 40), True), ((192, 192, 24), False)])
+def test_fused_transverse_passes_equal_the_three_pass_chain(shape, nonlinear, monkeypatch):
+    """The opt-in cluster kernels (CG_FUSED_XY=1) do the arithmetic of the y/x/y pass
+    sequence: same result to rounding."""
+    plan, grid, med, rng = _setup(shape, nonlinear, True, seed=3)
+    p0 = (rng.standard_normal((2,) + plan.padded) * 1e5).astype(np.float32).reshape(2, -1)
+    u0 = (rng.standard_normal((3, 2, plan.ncell)) * 0.05).astype(np.float32)
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("CG_FUSED_XY", flag)
+        with eng.DeviceSolver(plan, batch=2) as dev:
+            assert dev.launches_per_step == (4 if flag == "1" else 8)
+            dev.set_state(p0, u0, 0)
+            dev.run_steps(5)
+            out.append(dev.get_state())
+    (pa, ua), (pb, ub) = out
+    assert np.abs(pa - pb).max() / np.abs(pb).max() < 1e-6
+    assert np.abs(ua - ub).max() / np.abs(ub).max() < 1e-6
