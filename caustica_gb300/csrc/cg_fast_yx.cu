@@ -151,50 +151,56 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
       S0[base + (long long)(s + A * b) * ncol] = w[b];
     });
   } else if constexpr (MODE == X_GRAD) {
-    // S2 <- IFFT(kappa/N FFT(S0)); S1 <- IFFT(i kx kappa/N FFT(S0))
+    // S2 <- IFFT(q); S1 <- IFFT(i kx q), q = kappa/N FFT(S0); q waits in shared
+    // memory during the first inverse transform instead of in registers
+    float2* qs = sm + 2 * N + N * CG_XP;
     load(S0);
     fft2<A, B, false>(v, w, s, tw, exf);
     static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int k = (s < A) ? s + A * b : 0;
       w[b] = c_scale(w[b], kappa(k));
+      if (s < A) qs[(s + A * b) * CG_XP + c] = w[b];
     });
-#pragma unroll 1
-    for (int o = 0; o < 2; ++o) {
-      if (o == 1) static_for<0, B>([&](auto bi) {
-        constexpr int b = decltype(bi)::value;
-        const int k = (s < A) ? s + A * b : 0;
-        w[b] = c_muli(c_scale(w[b], t.kx[k]));
-      });
-      fft2<B, A, true>(w, z, s, twi, exi);
-      store_z(o == 0 ? S2 : S1);
-    }
+    fft2<B, A, true>(w, z, s, twi, exi);
+    store_z(S2);
+    static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      const int k = (s < A) ? s + A * b : 0;
+      w[b] = (s < A) ? c_muli(c_scale(qs[(s + A * b) * CG_XP + c], t.kx[k])) : make_float2(0.f, 0.f);
+    });
+    fft2<B, A, true>(w, z, s, twi, exi);
+    store_z(S1);
   } else {
-    // X_DIV: S0 <- IFFT(kappa/N (FFT(S0) + i kx FFT(S1)))
+    // X_DIV: S0 <- IFFT(kappa/N (FFT(S0) + i kx FFT(S1))); FFT(S1) waits in shared memory
+    float2* hs = sm + 2 * N + N * CG_XP;
     load(S1);
     fft2<A, B, false>(v, w, s, tw, exf);
-    float2 h[B];
-    static_for<0, B>([&](auto bi) { h[decltype(bi)::value] = w[decltype(bi)::value]; });
+    if (s < A) static_for<0, B>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      hs[(s + A * b) * CG_XP + c] = w[b];
+    });
     load(S0);
     fft2<A, B, false>(v, w, s, tw, exf);
     static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int k = (s < A) ? s + A * b : 0;
-      w[b] = c_scale(c_add(w[b], c_muli(c_scale(h[b], t.kx[k]))), kappa(k));
+      const float2 h = (s < A) ? hs[(s + A * b) * CG_XP + c] : make_float2(0.f, 0.f);
+      w[b] = c_scale(c_add(w[b], c_muli(c_scale(h, t.kx[k]))), kappa(k));
     });
     fft2<B, A, true>(w, z, s, twi, exi);
     store_z(S0);
   }
 }
 
-// twiddles | exchange
+// twiddles | exchange (| a parked x-spectrum tile)
 template <int N>
 static size_t smem_y() {
   return sizeof(float2) * (N + CG_YP * RowEx<Split<N>::A, Split<N>::B>::SLAB);
 }
 template <int N>
 static size_t smem_x() {
-  return sizeof(float2) * (2 * N + (size_t)N * CG_XP);
+  return sizeof(float2) * (2 * N + 2 * (size_t)N * CG_XP);  // + a parked spectrum tile
 }
 
 bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1, float2* S2, int batch,
