@@ -41,8 +41,10 @@ __global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(Dims d, T
   constexpr int A = Split<N>::A, B = Split<N>::B;
   using Ex = RowEx<A, B>;
   extern __shared__ float2 sm[];
+  cgf::pdl_trigger();
   float2* tw = sm;  // (A, B) order
   cgf::fill_twt<A, B>(tw, t.twy);
+  cgf::pdl_wait();
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
   const Ex ex{sm + N + p * Ex::SLAB};
   const long long nrows = (long long)d.nx * d.nzh;
@@ -109,10 +111,12 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
                                                          float2* __restrict__ S2) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
   extern __shared__ float2 sm[];
+  cgf::pdl_trigger();
   float2* tw = sm;       // (A, B) order
   float2* twi = sm + N;  // (B, A) order
   cgf::fill_twt<A, B>(tw, t.twx);
   cgf::fill_twt<B, A>(twi, t.twx);
+  cgf::pdl_wait();
   const int c = threadIdx.x % CG_XP, s = threadIdx.x / CG_XP;
   const ColEx<A, B, CG_XP> exf{sm + 2 * N + c};
   const ColEx<B, A, CG_XP> exi{sm + 2 * N + c};
@@ -210,10 +214,10 @@ bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1
 #define CASE(n)                                                                                            \
   case n:                                                                                                  \
     switch (mode) {                                                                                        \
-      case Y_FWD: kf_ypass<n, Y_FWD><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break;       \
-      case Y_INV: kf_ypass<n, Y_INV><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break;       \
-      case Y_INV_GRAD: kf_ypass<n, Y_INV_GRAD><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break; \
-      default: kf_ypass<n, Y_FWD_DIV><<<grid, 16 * CG_YP, smem_y<n>(), st>>>(d, t, S0, S1, S2); break;      \
+      case Y_FWD: cgf::launch(kf_ypass<n, Y_FWD>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break;       \
+      case Y_INV: cgf::launch(kf_ypass<n, Y_INV>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break;       \
+      case Y_INV_GRAD: cgf::launch(kf_ypass<n, Y_INV_GRAD>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break; \
+      default: cgf::launch(kf_ypass<n, Y_FWD_DIV>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break;      \
     }                                                                                                      \
     return true;
     CG_FAST_SIZES(CASE)
@@ -227,7 +231,7 @@ bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float inv
                 float2* S2, int batch, cudaStream_t st) {
   const dim3 grid((unsigned)(((long long)d.nzh * d.ny + CG_XP - 1) / CG_XP), batch);
   switch (d.nx) {
-#define XL(n, M) kf_xpass<n, M><<<grid, 16 * CG_XP, smem_x<n>(), st>>>(d, t, kcoef, invN, S0, S1, S2)
+#define XL(n, M) cgf::launch(kf_xpass<n, M>, grid, dim3(16 * CG_XP), smem_x<n>(), st, d, t, kcoef, invN, S0, S1, S2)
 #define CASE(n)                          \
   case n:                                \
     switch (mode) {                      \

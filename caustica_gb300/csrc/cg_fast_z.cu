@@ -171,12 +171,14 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_u(Dims d, T
   using Z = ZShape<N>;
   constexpr int A = Z::A, B = Z::B;
   extern __shared__ float2 sm[];
+  cgf::pdl_trigger();
   float2* tw = sm;        // (A, B) order: inverse transforms
   float2* twf = sm + N;   // (B, A) order: forward transforms
   float4* stg4 = reinterpret_cast<float4*>(sm + Z::OFF_STG);
   float2* xb = sm + Z::OFF_STG;
   cgf::fill_twt<A, B>(tw, t.twz);
   cgf::fill_twt<B, A>(twf, t.twz);
+  cgf::pdl_wait();
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
   const RowEx<A, B> exi{sm + Z::OFF_EX + p * Z::EX};
   const RowEx<B, A> exf{sm + Z::OFF_EX + p * Z::EX};
@@ -258,8 +260,10 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(Dims d, T
   float2* twf = sm + N;   // (B, A) order: forward transforms
   float4* stg4 = reinterpret_cast<float4*>(sm + Z::OFF_STG);
   float2* xb = sm + Z::OFF_STG;
+  cgf::pdl_trigger();
   cgf::fill_twt<A, B>(tw, t.twz);
   cgf::fill_twt<B, A>(twf, t.twz);
+  cgf::pdl_wait();
   if (threadIdx.x == 0) s_peak = 0u;
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
   const RowEx<A, B> exi{sm + Z::OFF_EX + p * Z::EX};
@@ -502,8 +506,10 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
   const long long total = per_member * n_members;
   const long long t0 = (long long)blockIdx.x * tiles_per_cta;
   const long long t1 = min(total, t0 + tiles_per_cta);
+  cgf::pdl_trigger();
   if (t0 >= t1) return;  // the whole CTA, before any barrier
   zp_tables<N>(sm, t, m);
+  cgf::pdl_wait();
   const float* kz_s = reinterpret_cast<const float*>(sm + Z::OFF_KZ);
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
@@ -597,8 +603,10 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, 
   const long long total = per_member * n_members;
   const long long t0 = (long long)blockIdx.x * tiles_per_cta;
   const long long t1 = min(total, t0 + tiles_per_cta);
+  cgf::pdl_trigger();
   if (t0 >= t1) return;  // the whole CTA, before any barrier
   zp_tables<N>(sm, t, m);
+  cgf::pdl_wait();
   if (threadIdx.x == 0) s_peak = 0u;
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
@@ -755,7 +763,7 @@ bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, 
     switch (d.nz) {
 #define CASE(n)                                                                                          \
   case n:                                                                                                \
-    kfp_zpass_u<n><<<g, CG_THREADS, ZPShape<n>::smem, st>>>(d, t, m, u, S0, S1, S2, batch, per);         \
+    cgf::launch(kfp_zpass_u<n>, dim3(g), dim3(CG_THREADS), ZPShape<n>::smem, st, d, t, m, u, S0, S1, S2, batch, per);         \
     return true;
       CG_FAST_SIZES(CASE)
 #undef CASE
@@ -766,7 +774,7 @@ bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, 
   switch (d.nz) {
 #define CASE(n)                                                                       \
   case n:                                                                             \
-    kf_zpass_u<n><<<grid, CG_THREADS, ZShape<n>::smem, st>>>(d, t, m, u, S0, S1, S2); \
+    cgf::launch(kf_zpass_u<n>, grid, dim3(CG_THREADS), ZShape<n>::smem, st, d, t, m, u, S0, S1, S2); \
     return true;
     CG_FAST_SIZES(CASE)
 #undef CASE
@@ -785,8 +793,8 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
     switch (d.nz) {
 #define CASE(n)                                                                                               \
   case n:                                                                                                     \
-    kfp_zpass_p<n><<<g, CG_THREADS, ZPShape<n>::smem, st>>>(d, t, m, src, rec, ctl, n_local, record, p, S0, \
-                                                            batch, per);                                      \
+    cgf::launch(kfp_zpass_p<n>, dim3(g), dim3(CG_THREADS), ZPShape<n>::smem, st, d, t, m, src, rec, ctl, n_local, \
+                record, p, S0, batch, per);                                      \
     return true;
       CG_FAST_SIZES(CASE)
 #undef CASE
@@ -796,7 +804,7 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
   }
   switch (d.nz) {
 #define ZL(n, M) \
-  kf_zpass_p<n, M><<<grid, CG_THREADS, ZShape<n>::smem, st>>>(d, t, m, src, rec, ctl, n_local, record, p, S0)
+  cgf::launch(kf_zpass_p<n, M>, grid, dim3(CG_THREADS), ZShape<n>::smem, st, d, t, m, src, rec, ctl, n_local, record, p, S0)
 #define CASE(n)                                         \
   case n:                                               \
     if (mode == 0) ZL(n, 0);                            \
