@@ -425,8 +425,10 @@ struct ZPShape {
   static constexpr int B_MAX = B_STG > B_EX ? (B_STG > B_XB ? B_STG : B_XB) : (B_EX > B_XB ? B_EX : B_XB);
   static constexpr int BUF = (B_MAX + 1) / 2 * 2;  // even: float4-aligned
   static constexpr int KZF = (NH + 3) / 4 * 2;     // k_z table (floats), float2 units, even
-  // twiddles (two orders) | k_z | two item buffers | material table | two label tiles
-  static constexpr size_t OFF_KZ = 2 * N, OFF_BUF = OFF_KZ + KZF, OFF_TAB = OFF_BUF + 2 * (size_t)BUF;
+  static constexpr int SZF = (N + 3) / 4 * 2;      // z sponge profile (floats), float2 units, even
+  // twiddles (two orders) | k_z | z sponge | two item buffers | material table | two label tiles
+  static constexpr size_t OFF_KZ = 2 * N, OFF_SZ = OFF_KZ + KZF, OFF_BUF = OFF_SZ + SZF;
+  static constexpr size_t OFF_TAB = OFF_BUF + 2 * (size_t)BUF;
   static constexpr size_t OFF_LAB = OFF_TAB + 2 * 256;
   static constexpr size_t smem = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
 };
@@ -488,6 +490,8 @@ __device__ __forceinline__ void zp_tables(float2* sm, const Tables& t, const Med
   cgf::fill_twt<Z::B, Z::A>(sm + N, t.twz);
   float* kz_s = reinterpret_cast<float*>(sm + Z::OFF_KZ);
   for (int i = threadIdx.x; i < Z::NH; i += blockDim.x) kz_s[i] = t.kz[i];
+  float* sz_s = reinterpret_cast<float*>(sm + Z::OFF_SZ);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) sz_s[i] = t.sz[i];
   float4* tab_s = reinterpret_cast<float4*>(sm + Z::OFF_TAB);
   if (m.labels)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) tab_s[i] = m.ltab[i];
@@ -511,6 +515,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
   zp_tables<N>(sm, t, m);
   cgf::pdl_wait();
   const float* kz_s = reinterpret_cast<const float*>(sm + Z::OFF_KZ);
+  const float* sz_s = reinterpret_cast<const float*>(sm + Z::OFF_SZ);
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
@@ -567,7 +572,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
       if (s < A) static_for<0, B>([&](auto bi) {
         constexpr int b = decltype(bi)::value;
         const int n = s + A * b;
-        const float sz = t.sz[n];
+        const float sz = sz_s[n];
         const float4 ca = lab ? tab_s[la[n]] : cell_coef(m, rowa + n);
         const float4 cb = lab ? tab_s[lb[n]] : cell_coef(m, rowb + n);
         float una = ua[b] - ca.x * w[b].x;
@@ -608,6 +613,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, 
   zp_tables<N>(sm, t, m);
   cgf::pdl_wait();
   if (threadIdx.x == 0) s_peak = 0u;
+  const float* sz_s = reinterpret_cast<const float*>(sm + Z::OFF_SZ);
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
@@ -659,7 +665,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, 
     if (s < A) static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
-      const float sz = t.sz[n];
+      const float sz = sz_s[n];
       const float4 ca = lab ? tab_s[la[n]] : cell_coef(m, rowa + n);
       const float4 cb = lab ? tab_s[lb[n]] : cell_coef(m, rowb + n);
       const float poa = pa[b], pob = pbv[b];
