@@ -116,6 +116,11 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
   float2* twi = sm + N;  // (B, A) order
   cgf::fill_twt<A, B>(tw, t.twx);
   cgf::fill_twt<B, A>(twi, t.twx);
+  float* kxs = reinterpret_cast<float*>(sm + 2 * N + 2 * N * CG_XP);  // k_x | k_x^2
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    kxs[i] = t.kx[i];
+    kxs[N + i] = t.kx2[i];
+  }
   cgf::pdl_wait();
   const int c = threadIdx.x % CG_XP, s = threadIdx.x / CG_XP;
   const ColEx<A, B, CG_XP> exf{sm + 2 * N + c};
@@ -146,7 +151,7 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
       dst[base + (long long)(s + B * a) * ncol] = z[a];
     });
   };
-  auto kappa = [&](int k) { return sinc_a2(kcoef * (t.kx2[k] + kyz2)) * invN; };
+  auto kappa = [&](int k) { return sinc_a2(kcoef * (kxs[N + k] + kyz2)) * invN; };
   if constexpr (MODE == X_FWD || MODE == X_INV) {
     load(S0);
     fft2<A, B, MODE == X_INV>(v, w, s, tw, exf);
@@ -171,7 +176,7 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
     static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int k = (s < A) ? s + A * b : 0;
-      w[b] = (s < A) ? c_muli(c_scale(qs[(s + A * b) * CG_XP + c], t.kx[k])) : make_float2(0.f, 0.f);
+      w[b] = (s < A) ? c_muli(c_scale(qs[(s + A * b) * CG_XP + c], kxs[k])) : make_float2(0.f, 0.f);
     });
     fft2<B, A, true>(w, z, s, twi, exi);
     store_z(S1);
@@ -190,21 +195,21 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
       constexpr int b = decltype(bi)::value;
       const int k = (s < A) ? s + A * b : 0;
       const float2 h = (s < A) ? hs[(s + A * b) * CG_XP + c] : make_float2(0.f, 0.f);
-      w[b] = c_scale(c_add(w[b], c_muli(c_scale(h, t.kx[k]))), kappa(k));
+      w[b] = c_scale(c_add(w[b], c_muli(c_scale(h, kxs[k]))), kappa(k));
     });
     fft2<B, A, true>(w, z, s, twi, exi);
     store_z(S0);
   }
 }
 
-// twiddles | exchange (| a parked x-spectrum tile)
+// twiddles | exchange | (x: a parked spectrum tile, k_x, k_x^2)
 template <int N>
 static size_t smem_y() {
   return sizeof(float2) * (N + CG_YP * RowEx<Split<N>::A, Split<N>::B>::SLAB);
 }
 template <int N>
 static size_t smem_x() {
-  return sizeof(float2) * (2 * N + 2 * (size_t)N * CG_XP);  // + a parked spectrum tile
+  return sizeof(float2) * (2 * N + 2 * (size_t)N * CG_XP) + 2 * sizeof(float) * N;  // + parked tile, k_x, k_x^2
 }
 
 bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1, float2* S2, int batch,
