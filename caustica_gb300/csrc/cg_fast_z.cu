@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
       });
       float2 X[A];
       fft2<B, A, false>(w, X, s, sm + N, exf);
-      z_split_store<N>(bufj, X, spec(comp, b_idx), d, x, y0, p, s, comp == 2 ? t.kz : nullptr);
+      z_split_store<N>(bufj, X, spec(comp, b_idx), d, x, y0, p, s, comp == 2 ? kz_s : nullptr);
     }
   }
 }
