@@ -325,4 +325,26 @@ inline void launch(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cuda
   cudaLaunchKernelEx(&cfg, k, args...);
 }
 
+// SM count of the current device (cached; 152 on GB300 if the query fails).
+inline int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n < 1)
+      n = 152;
+  }
+  return n;
+}
+
+// Persistent grid over `total` equal work items: about `per_sm` CTAs per SM,
+// each a contiguous run of *per_cta items, none empty.
+inline void persistent_grid(long long total, int per_sm, int* grid, int* per_cta) {
+  const long long slots = (long long)sm_count() * per_sm;
+  const long long g0 = total < slots ? total : slots;
+  const long long per = (total + g0 - 1) / g0;
+  *per_cta = (int)per;
+  *grid = (int)((total + per - 1) / per);
+}
+
 }  // namespace cgf

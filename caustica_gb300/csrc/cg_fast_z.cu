@@ -741,31 +741,12 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, 
   }
 }
 
-static int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
-      n = 152;
-  }
-  return n;
-}
-
-// Persistent grid: about CG_FAST_MINB CTAs per SM, every CTA a run of equal length.
-static void persistent_grid(long long total, int* grid, int* per_cta) {
-  const long long slots = (long long)sm_count() * CG_FAST_MINB;
-  const long long g0 = total < slots ? total : slots;
-  const long long per = (total + g0 - 1) / g0;
-  *per_cta = (int)per;
-  *grid = (int)((total + per - 1) / per);
-}
-
 bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
                   int batch, cudaStream_t st) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
   if (d.ny % CG_ZROWS == 0) {
     int g = 0, per = 0;
-    persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, &g, &per);
+    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, CG_FAST_MINB, &g, &per);
     switch (d.nz) {
 #define CASE(n)                                                                                          \
   case n:                                                                                                \
@@ -795,7 +776,7 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
   if (mode == 1 && d.ny % CG_ZROWS == 0) {
     int g = 0, per = 0;
-    persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, &g, &per);
+    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, CG_FAST_MINB, &g, &per);
     switch (d.nz) {
 #define CASE(n)                                                                                               \
   case n:                                                                                                     \
