@@ -163,6 +163,19 @@ def _traffic_from_profiles(kernel: str):
 
 SLOTS = ["k_ypass:fwd", "k_xpass:grad", "k_ypass:inv_grad", "k_zpass_u", "k_ypass:fwd_div", "k_xpass:div",
          "k_ypass:inv", "k_zpass_p"]
+FAST_SIZES = {8, 16, 24, 32, 48, 64, 96, 128, 160, 192, 256}
+
+
+def slot_symbols(padded3) -> list[str]:
+    """The kernel each step slot launches on this grid (size-specialised where the axis allows)."""
+    nx, ny, nz = padded3
+    y = f"kf_ypass<{ny},{{}}>" if ny in FAST_SIZES else "k_ypass"
+    x = f"kf_xpass<{nx},{{}}>" if nx in FAST_SIZES else "k_xpass"
+    zp = "kfp" if ny % 32 == 0 else "kf"
+    zu = f"{zp}_zpass_u<{nz}>" if nz in FAST_SIZES else "k_zpass_u"
+    zpp = (f"{zp}_zpass_p<{nz}>" if zp == "kfp" else f"kf_zpass_p<{nz},1>") if nz in FAST_SIZES else "k_zpass_p"
+    return [y.format("Y_FWD"), x.format("X_GRAD"), y.format("Y_INV_GRAD"), zu, y.format("Y_FWD_DIV"),
+            x.format("X_DIV"), y.format("Y_INV"), zpp]
 
 
 def slot_bytes(ncell: int, nspec: int, labels: bool, nonlinear: bool, record: bool = False) -> list[int]:
@@ -255,6 +268,7 @@ def run_gb300(args, dist, rank, ws, local):
     K, W = int(args.steps), int(args.warmup)
     graph = K % plan.spp == 0 and W % plan.spp == 0
     dev = eng.DeviceSolver(plan)
+    launches_per_step = dev.launches_per_step
     try:
         # drive table long enough that the source keeps injecting through the timed steps
         dev.extend_drive((plan.eff_min + 4) * plan.spp + W + 2 * K)
@@ -300,14 +314,15 @@ def run_gb300(args, dist, rank, ws, local):
                        "timing": "CUDA events on the solver stream, " + ("CUDA graph per period" if graph else
                                                                            "direct launches"),
                        "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush"},
-            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "kernel": kernel_name, "kernel_symbol": slot_symbols(plan.padded3)[dom],
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_launch": bytes_slot[dom],
                          "ms_per_launch": float(per_launch_ms[dom]), "traffic": traffic},
             "step_roofline": {"bytes_per_cell_step": step_b, "achieved": step_achieved, "peak": hbm,
                               "frac": step_achieved / hbm, "unit": "GB/s",
                               "note": "algorithmic bytes of the fully fused step with label-indexed maps"},
             "profile_ms_per_launch": {SLOTS[i]: float(per_launch_ms[i]) for i in range(8)},
-            "gpu_launches": K * 8 + (K // plan.spp if graph else 1)}
+            "gpu_launches": K * launches_per_step + (K // plan.spp if graph else 1)}
 
     # end-to-end: one full solve through the public solver front, host numpy in, host numpy out
     if not args.skip_e2e:
