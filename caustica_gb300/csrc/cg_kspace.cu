@@ -515,25 +515,41 @@ __global__ void __launch_bounds__(CG_THREADS) k_zpass_p(int mode, Dims d, AxisPl
 
 // Final phasors in FP64: P_h = 2/K sum_m (s_m - c_m) exp(+2 pi i h m / spp)
 // (engine.py:538-552: buffers[h] += p exp(+i h w t); *= 2/rec_steps).
+// The nh x spp unit phasors are formed once per block in shared memory (FP64
+// sincospi is slow on GB300); every bin is read once and feeds all
+// harmonics, each summed over m in increasing order.
 __global__ void k_finalize(RecordDev rec, int B, int nh, const int* harm, int K, float2* out) {
-  long long total = (long long)B * rec.nrec;
+  extern __shared__ double2 uph[];  // [nh][spp] (cos, sin)
+  for (int i = threadIdx.x; i < nh * rec.spp; i += blockDim.x) {
+    const int h = i / rec.spp, mm = i - h * rec.spp;
+    double sn, cs;
+    sincospi(2.0 * (double)((harm[h] * (long long)mm) % rec.spp) / rec.spp, &sn, &cs);
+    uph[i] = make_double2(cs, sn);
+  }
+  __syncthreads();
+  const long long total = (long long)B * rec.nrec;
+  const double sc = 2.0 / K;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
-    long long b = i / rec.nrec;
-    long long r = i - b * rec.nrec;
-    for (int h = 0; h < nh; ++h) {
-      double re = 0.0, im = 0.0;
-      for (int mm = 0; mm < rec.spp; ++mm) {
-        long long o = (b * rec.spp + mm) * rec.nrec + r;
-        double v = (double)rec.bins[o] - (double)rec.comp[o];
-        double sn, cs;
-        sincospi(2.0 * (double)((harm[h] * (long long)mm) % rec.spp) / rec.spp, &sn, &cs);
-        re += v * cs;
-        im += v * sn;
-      }
-      double sc = 2.0 / K;
-      out[(b * nh + h) * rec.nrec + r] = make_float2((float)(re * sc), (float)(im * sc));
+    const long long b = i / rec.nrec;
+    const long long r = i - b * rec.nrec;
+    double re[CG_MAX_H], im[CG_MAX_H];
+#pragma unroll
+    for (int h = 0; h < CG_MAX_H; ++h) re[h] = im[h] = 0.0;
+    for (int mm = 0; mm < rec.spp; ++mm) {
+      const long long o = (b * rec.spp + mm) * rec.nrec + r;
+      const double v = (double)rec.bins[o] - (double)rec.comp[o];
+#pragma unroll
+      for (int h = 0; h < CG_MAX_H; ++h)
+        if (h < nh) {
+          const double2 u = uph[h * rec.spp + mm];
+          re[h] += v * u.x;
+          im[h] += v * u.y;
+        }
     }
+#pragma unroll
+    for (int h = 0; h < CG_MAX_H; ++h)
+      if (h < nh) out[(b * nh + h) * rec.nrec + r] = make_float2((float)(re[h] * sc), (float)(im[h] * sc));
   }
 }
 
@@ -702,6 +718,9 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
              cfg->nx, cfg->ny, cfg->nz);
   CG_REQUIRE(cfg->batch >= 1 && cfg->batch <= 65535, "batch %d out of range", cfg->batch);
   CG_REQUIRE(cfg->spp >= 2, "spp must be >= 2");
+  CG_REQUIRE((long long)cfg->spp * (cfg->n_harmonics > 0 ? cfg->n_harmonics : 1) <= 8192,
+             "spp x n_harmonics must be <= 8192 (the finalize unit-phasor table), got %d x %d", cfg->spp,
+             cfg->n_harmonics);
   CG_REQUIRE(cfg->n_harmonics >= 1 && cfg->n_harmonics <= CG_MAX_H, "n_harmonics must be 1..%d", CG_MAX_H);
   CG_REQUIRE(cfg->max_periods >= 1, "max_periods must be >= 1");
   cg_solver* s = new cg_solver();
@@ -805,6 +824,7 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_xpass);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_zpass_u);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_zpass_p);
+  if (e == cudaSuccess) e = allow_max_smem((const void*)k_finalize);
   if (e == cudaSuccess && fast_prepare() != 0) e = cudaErrorInvalidValue;
   if (e != cudaSuccess) {
     cg_set_error("solver set-up: %s", cudaGetErrorString(e));
@@ -1114,7 +1134,8 @@ extern "C" int cg_solver_finalize(cg_solver* s, int n_record_steps, float* phaso
     int rc = dev_alloc(&s->ph, (size_t)s->B * s->nh * s->nrec);
     if (rc != CG_OK) return rc;
   }
-  k_finalize<<<1024, 256, 0, s->stream>>>(make_record(s), s->B, s->nh, s->harm_dev, n_record_steps, s->ph);
+  k_finalize<<<1024, 256, sizeof(double2) * (size_t)s->nh * s->spp, s->stream>>>(make_record(s), s->B, s->nh,
+                                                                                  s->harm_dev, n_record_steps, s->ph);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && phasors)
     e = cudaMemcpyAsync(phasors, s->ph, sizeof(float2) * (size_t)s->B * s->nh * s->nrec, cudaMemcpyDefault,

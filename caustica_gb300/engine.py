@@ -126,28 +126,61 @@ def _first_occurrence(inv: np.ndarray, n: int, chunk: int = 1 << 20) -> np.ndarr
     return first
 
 
+def _labels_match(props: np.ndarray, inv: np.ndarray, vols) -> bool:
+    """props[inv] == vols bit for bit, checked in chunks on a few host threads
+    (the NumPy gathers and compares release the GIL)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    flat = [v.reshape(-1).view(np.uint32) for v in vols]
+    luts = [np.ascontiguousarray(props[:, i]).view(np.uint32) for i in range(len(vols))]
+    n = inv.size
+    nt = max(1, min(8, os.cpu_count() or 1))
+    step = max(1 << 16, (n + 4 * nt - 1) // (4 * nt))
+
+    def chunk(a):
+        b = min(n, a + step)
+        return all(np.array_equal(np.take(lut, inv[a:b]), f[a:b]) for lut, f in zip(luts, flat))
+
+    if n <= step:
+        return chunk(0)
+    with ThreadPoolExecutor(nt) as ex:
+        return all(ex.map(chunk, range(0, n, step)))
+
+
 def label_volumes(vols, id_map=None, max_labels: int = 256):
     """Exact label decomposition of equally shaped float32 volumes.
 
     Returns ``(labels uint8, props (n, len(vols)) float32)`` when at most
     ``max_labels`` distinct value tuples occur (``props[labels] == vols``),
-    else None. An integer ``id_map`` is tried first (O(N)).
+    else None. An integer ``id_map`` is tried first (O(N)); ids spanning at
+    most ``max_labels`` values become labels directly (id - min), the rows
+    of ids that do not occur repeat an occurring row.
     """
     vols = [np.ascontiguousarray(v, np.float32) for v in vols]
     nv = len(vols)
     if id_map is not None:
         ids_flat = np.asarray(id_map).reshape(-1)
-        lo, hi = int(ids_flat.min()), int(ids_flat.max())
-        if hi - lo < (1 << 20):
-            present = np.flatnonzero(np.bincount(ids_flat - lo, minlength=hi - lo + 1))
-            if len(present) <= max_labels:
-                lut = np.zeros(hi - lo + 1, np.int64)
-                lut[present] = np.arange(len(present))
-                inv = lut[ids_flat - lo]
-                first = _first_occurrence(inv, len(present))
-                props = np.stack([v.reshape(-1)[first] for v in vols], axis=1)
-                if all(np.array_equal(props[inv, i], vols[i].reshape(-1)) for i in range(nv)):
-                    return inv.astype(np.uint8).reshape(vols[0].shape), props.astype(np.float32)
+        if ids_flat.size == vols[0].size and ids_flat.dtype.kind in "iu":
+            lo, hi = int(ids_flat.min()), int(ids_flat.max())
+            if hi - lo < max_labels:
+                inv = (ids_flat - lo).astype(np.uint8) if lo else ids_flat.astype(np.uint8)
+                n = hi - lo + 1
+                first = _first_occurrence(inv, n)
+                first[first < 0] = first[first >= 0][0]
+                props = np.stack([v.reshape(-1)[first] for v in vols], axis=1).astype(np.float32)
+                if _labels_match(props, inv, vols):
+                    return inv.reshape(vols[0].shape), props
+            elif hi - lo < (1 << 20):
+                present = np.flatnonzero(np.bincount(ids_flat - lo, minlength=hi - lo + 1))
+                if len(present) <= max_labels:
+                    lut = np.zeros(hi - lo + 1, np.uint8)
+                    lut[present] = np.arange(len(present))
+                    inv = lut[ids_flat - lo]
+                    first = _first_occurrence(inv, len(present))
+                    props = np.stack([v.reshape(-1)[first] for v in vols], axis=1).astype(np.float32)
+                    if _labels_match(props, inv, vols):
+                        return inv.reshape(vols[0].shape), props
     flat = [v.reshape(-1) for v in vols]
     if all(np.all(f == f[0]) for f in flat):
         return (np.zeros(vols[0].shape, np.uint8),
