@@ -8,18 +8,18 @@
 #include "cg_fast.cuh"
 #include "cg_kspace.cuh"
 
-// resident CTAs per SM the register allocation targets (y: 8-row CTAs,
+// resident CTAs per SM the register allocation targets (y: 4-row CTAs,
 // ~102 registers per thread, no spills; x: 16-column CTAs, ~85 registers;
 // both measured best on a 192^2 x 256 grid)
 #ifndef CG_FAST_MINB_Y
-#define CG_FAST_MINB_Y 5
+#define CG_FAST_MINB_Y 10
 #endif
 #ifndef CG_FAST_MINB_X
 #define CG_FAST_MINB_X 3
 #endif
 // rows per y-CTA and columns per x-CTA (16 threads each)
 #ifndef CG_YP
-#define CG_YP 8
+#define CG_YP 4
 #endif
 #ifndef CG_XP
 #define CG_XP 16
