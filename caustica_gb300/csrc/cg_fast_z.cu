@@ -428,8 +428,9 @@ struct ZPShape {
   static constexpr int SZF = (N + 3) / 4 * 2;      // z sponge profile (floats), float2 units, even
   // twiddles (two orders) | k_z | z sponge | two item buffers | material table | two label tiles
   static constexpr size_t OFF_KZ = 2 * N, OFF_SZ = OFF_KZ + KZF, OFF_BUF = OFF_SZ + SZF;
-  static constexpr size_t OFF_TAB = OFF_BUF + 2 * (size_t)BUF;
-  static constexpr size_t OFF_LAB = OFF_TAB + 2 * 256;
+  static constexpr size_t OFF_TAB = OFF_BUF + 2 * (size_t)BUF;  // float4 per material
+  static constexpr size_t OFF_TAB2 = OFF_TAB + 2 * 256;          // float2 (dt/rho, absorb) per material
+  static constexpr size_t OFF_LAB = OFF_TAB2 + 256;
   static constexpr size_t smem = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
 };
 
@@ -493,8 +494,13 @@ __device__ __forceinline__ void zp_tables(float2* sm, const Tables& t, const Med
   float* sz_s = reinterpret_cast<float*>(sm + Z::OFF_SZ);
   for (int i = threadIdx.x; i < N; i += blockDim.x) sz_s[i] = t.sz[i];
   float4* tab_s = reinterpret_cast<float4*>(sm + Z::OFF_TAB);
+  float2* tab2_s = sm + Z::OFF_TAB2;
   if (m.labels)
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) tab_s[i] = m.ltab[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+      const float4 c = m.ltab[i];
+      tab_s[i] = c;
+      tab2_s[i] = make_float2(c.x, c.z);
+    }
 }
 
 template <int N>
@@ -516,7 +522,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
   cgf::pdl_wait();
   const float* kz_s = reinterpret_cast<const float*>(sm + Z::OFF_KZ);
   const float* sz_s = reinterpret_cast<const float*>(sm + Z::OFF_SZ);
-  const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
+  const float2* tab2_s = sm + Z::OFF_TAB2;
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
@@ -573,13 +579,14 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
         constexpr int b = decltype(bi)::value;
         const int n = s + A * b;
         const float sz = sz_s[n];
-        const float4 ca = lab ? tab_s[la[n]] : cell_coef(m, rowa + n);
-        const float4 cb = lab ? tab_s[lb[n]] : cell_coef(m, rowb + n);
+        // (dt/rho, absorb) of the two cells
+        const float2 ca = lab ? tab2_s[la[n]] : make_float2(m.dtr[rowa + n], m.ab[rowa + n]);
+        const float2 cb = lab ? tab2_s[lb[n]] : make_float2(m.dtr[rowb + n], m.ab[rowb + n]);
         float una = ua[b] - ca.x * w[b].x;
-        una = una * ca.z;
+        una = una * ca.y;
         una = una * (spa * sz);
         float unb = ub[b] - cb.x * w[b].y;
-        unb = unb * cb.z;
+        unb = unb * cb.y;
         unb = unb * (spb * sz);
         uc[rowa + n] = una;
         uc[rowb + n] = unb;
