@@ -22,6 +22,19 @@ using cgf::Split;
 using cgf::fft2;
 using cgf::static_for;
 
+// Pencil split of the z-transforms: (A, B) of the inverse transform (B
+// threads hold A values on input, A threads hold B values on output).
+// Lengths with a 16-point factor and a co-factor <= 16 use Split<N> on 16
+// threads per pencil; 320 = 16 x 20 runs on 20 threads per pencil.
+template <int N>
+struct ZSplit {
+  static constexpr int A = Split<N>::A, B = Split<N>::B;
+};
+template <>
+struct ZSplit<320> {
+  static constexpr int A = 16, B = 20;
+};
+
 template <int N>
 struct ZShape {
   static constexpr int A = Split<N>::A, B = Split<N>::B, NH = N / 2 + 1;
@@ -131,9 +144,9 @@ __device__ __forceinline__ void z_inputs(float2 (&v)[Split<N>::A], const float4*
 // xb[k * 17 + p], then split each pencil into its two half spectra and store
 // them to S (x, k, y0 + 2p + {0, 1}), times i*mk[k] when given.
 template <int N>
-__device__ __forceinline__ void z_split_store(float2* xb, const float2 (&X)[Split<N>::A], float2* __restrict__ S,
+__device__ __forceinline__ void z_split_store(float2* xb, const float2 (&X)[ZSplit<N>::A], float2* __restrict__ S,
                                               const Dims& d, int x, int y0, int p, int s, const float* mk) {
-  constexpr int A = Split<N>::A, B = Split<N>::B, NH = N / 2 + 1;
+  constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B, NH = N / 2 + 1;
   if (s < B) static_for<0, A>([&](auto ai) {
     constexpr int a = decltype(ai)::value;
     xb[(s + B * a) * 17 + p] = X[a];
@@ -418,7 +431,10 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(Dims d, T
 // fit on an SM.
 template <int N>
 struct ZPShape {
-  static constexpr int A = Split<N>::A, B = Split<N>::B, NH = N / 2 + 1;
+  static constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B, NH = N / 2 + 1;
+  static constexpr int TPP = A > B ? A : B;              // threads per pencil
+  static constexpr int THREADS = CG_TILE * TPP;
+  static constexpr int MINB = TPP == 16 ? CG_FAST_MINB : 1;  // resident CTAs per SM
   static constexpr int EX_I = RowEx<A, B>::SLAB, EX_F = RowEx<B, A>::SLAB;
   static constexpr int EX = EX_I > EX_F ? EX_I : EX_F;
   static constexpr int B_STG = NH * 34, B_EX = CG_TILE * EX, B_XB = N * 17;  // float2 units
@@ -456,9 +472,9 @@ __device__ __forceinline__ void z_prefetch_labels(uint8_t* lab_s, const uint8_t*
 // z_inputs on a raw staged tile: times i*mk[k] when mk is given, Im of the
 // self-paired bins dropped, then the Hermitian extension.
 template <int N>
-__device__ __forceinline__ void z_inputs_raw(float2 (&v)[Split<N>::A], const float4* stg4, int p, int s,
+__device__ __forceinline__ void z_inputs_raw(float2 (&v)[ZSplit<N>::A], const float4* stg4, int p, int s,
                                              const float* mk) {
-  constexpr int A = Split<N>::A, B = Split<N>::B;
+  constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B;
   static_for<0, A>([&](auto ai) {
     constexpr int a = decltype(ai)::value;
     const int n = s + B * a;
@@ -504,7 +520,7 @@ __device__ __forceinline__ void zp_tables(float2* sm, const Tables& t, const Med
 }
 
 template <int N>
-__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, Tables t, MediumDev m,
+__global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpass_u(Dims d, Tables t, MediumDev m,
                                                                        float* __restrict__ u, float2* __restrict__ S0,
                                                                        float2* __restrict__ S1, float2* __restrict__ S2,
                                                                        int n_members, int tiles_per_cta) {
@@ -525,7 +541,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
   const float2* tab2_s = sm + Z::OFF_TAB2;
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
-  const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
+  const int s = threadIdx.x % Z::TPP, p = threadIdx.x / Z::TPP;
   auto spec = [&](int comp, long long b) { return (comp == 0 ? S1 : (comp == 1 ? S0 : S2)) + b * d.nspec; };
   auto prefetch = [&](long long tile, int comp, int j) {
     const long long b = tile / per_member, r = tile - b * per_member;
@@ -600,7 +616,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_u(Dims d, 
 }
 
 template <int N>
-__global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, Tables t, MediumDev m,
+__global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpass_p(Dims d, Tables t, MediumDev m,
                                                                        SourceDev src, RecordDev rec,
                                                                        const long long* ctl, int n_local, int record,
                                                                        float* __restrict__ p_all,
@@ -624,7 +640,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kfp_zpass_p(Dims d, 
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
-  const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
+  const int s = threadIdx.x % Z::TPP, p = threadIdx.x / Z::TPP;
   auto prefetch = [&](long long tile, int j) {
     const long long b = tile / per_member, r = tile - b * per_member;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
@@ -753,13 +769,14 @@ bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, 
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
   if (d.ny % CG_ZROWS == 0) {
     int g = 0, per = 0;
-    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, CG_FAST_MINB, &g, &per);
     switch (d.nz) {
-#define CASE(n)                                                                                          \
-  case n:                                                                                                \
-    cgf::launch(kfp_zpass_u<n>, dim3(g), dim3(CG_THREADS), ZPShape<n>::smem, st, d, t, m, u, S0, S1, S2, batch, per);         \
+#define CASE(n)                                                                                            \
+  case n:                                                                                                  \
+    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, ZPShape<n>::MINB, &g, &per);         \
+    cgf::launch(kfp_zpass_u<n>, dim3(g), dim3(ZPShape<n>::THREADS), ZPShape<n>::smem, st, d, t, m, u, S0, S1, \
+                S2, batch, per);                                                                           \
     return true;
-      CG_FAST_SIZES(CASE)
+      CG_FAST_ZSIZES(CASE)
 #undef CASE
       default:
         return false;
@@ -783,14 +800,14 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
   if (mode == 1 && d.ny % CG_ZROWS == 0) {
     int g = 0, per = 0;
-    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, CG_FAST_MINB, &g, &per);
     switch (d.nz) {
 #define CASE(n)                                                                                               \
   case n:                                                                                                     \
-    cgf::launch(kfp_zpass_p<n>, dim3(g), dim3(CG_THREADS), ZPShape<n>::smem, st, d, t, m, src, rec, ctl, n_local, \
-                record, p, S0, batch, per);                                      \
+    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, ZPShape<n>::MINB, &g, &per);            \
+    cgf::launch(kfp_zpass_p<n>, dim3(g), dim3(ZPShape<n>::THREADS), ZPShape<n>::smem, st, d, t, m, src, rec,  \
+                ctl, n_local, record, p, S0, batch, per);                                                      \
     return true;
-      CG_FAST_SIZES(CASE)
+      CG_FAST_ZSIZES(CASE)
 #undef CASE
       default:
         return false;
@@ -822,14 +839,18 @@ int fast_prepare_z() {
       cudaFuncSetAttribute(kf_zpass_p<n, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
           cudaSuccess ||                                                                                \
       cudaFuncSetAttribute(kf_zpass_p<n, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZShape<n>::smem) != \
-          cudaSuccess ||                                                                                \
-      cudaFuncSetAttribute(kfp_zpass_u<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZPShape<n>::smem) != \
-          cudaSuccess ||                                                                                \
-      cudaFuncSetAttribute(kfp_zpass_p<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZPShape<n>::smem) != \
           cudaSuccess)                                                                                  \
     return -1;
   CG_FAST_SIZES(SET)
 #undef SET
+#define SETP(n)                                                                                          \
+  if (cudaFuncSetAttribute(kfp_zpass_u<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZPShape<n>::smem) != \
+          cudaSuccess ||                                                                                 \
+      cudaFuncSetAttribute(kfp_zpass_p<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZPShape<n>::smem) != \
+          cudaSuccess)                                                                                   \
+    return -1;
+  CG_FAST_ZSIZES(SETP)
+#undef SETP
   return 0;
 }
 
