@@ -269,6 +269,7 @@ def run_gb300(args, dist, rank, ws, local):
     graph = K % plan.spp == 0 and W % plan.spp == 0
     dev = eng.DeviceSolver(plan)
     launches_per_step = dev.launches_per_step
+    tuning = dev.tuning
     try:
         # drive table long enough that the source keeps injecting through the timed steps
         dev.extend_drive((plan.eff_min + 4) * plan.spp + W + 2 * K)
@@ -313,7 +314,8 @@ def run_gb300(args, dist, rank, ws, local):
                        "source_voxels": int(plan.src_xyz.shape[0]), "spp": plan.spp,
                        "timing": "CUDA events on the solver stream, " + ("CUDA graph per period" if graph else
                                                                            "direct launches"),
-                       "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush"},
+                       "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush",
+                       "tuning": tuning},
             "roofline": {"bound": "hbm", "kernel": kernel_name, "kernel_symbol": slot_symbols(plan.padded3)[dom],
                          "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_launch": bytes_slot[dom],

@@ -23,6 +23,9 @@
 //   Yinv(S0) -> Zp(p update, source, peak, record, R2C p -> S0)
 // The 1/N of the inverse transforms is folded into kappa.
 #include <math.h>
+
+#include <map>
+#include <mutex>
 #include <stdarg.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1031,7 +1034,7 @@ static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = 
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
   }
   EV(3);
-  if (!fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st))
+  if (!fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, s->zpers != 0))
     k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
   EV(4);
   if (fx) {
@@ -1052,7 +1055,8 @@ static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = 
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
   }
   EV(7);
-  if (!fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st))
+  if (!fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st,
+                    s->zpers != 0))
     k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
                                                  record, s->p, s->S0);
   EV(8);
@@ -1237,6 +1241,98 @@ extern "C" int cg_solver_timed_run(cg_solver* s, int n_steps, int record, int gr
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return rc;
+}
+
+// ------------------------------------------------------------ autotuner --
+// Per (grid, batch, physics, medium storage): time every launch configuration
+// the grid admits -- fused or three-pass transverse chain, persistent or
+// one-tile-per-CTA z-passes -- over a few steps of the handle itself, keep
+// the fastest, and remember it for the process. The handle must be fresh
+// (the trial steps run on its state, which is reset afterwards).
+namespace {
+struct TuneKey {
+  int nx, ny, nz, B, nonlinear, labels;
+  bool operator<(const TuneKey& o) const {
+    const int a[6] = {nx, ny, nz, B, nonlinear, labels}, b[6] = {o.nx, o.ny, o.nz, o.B, o.nonlinear, o.labels};
+    for (int i = 0; i < 6; ++i)
+      if (a[i] != b[i]) return a[i] < b[i];
+    return false;
+  }
+};
+std::map<TuneKey, std::pair<int, int>> g_tuned;
+std::mutex g_tune_mu;
+}  // namespace
+
+extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
+  CG_REQUIRE(s && out4, "null argument");
+  CG_REQUIRE(s->has_medium, "set a medium before tuning");
+  CG_REQUIRE(n_steps >= 1, "n_steps must be >= 1");
+  const TuneKey key{s->d.nx, s->d.ny, s->d.nz, s->B, s->nonlinear, s->labels != nullptr};
+  // CG_FUSED_XY=0 / =1 pin the transverse chain (comparison runs): no cache
+  const char* fenv = getenv("CG_FUSED_XY");
+  const bool pinned = fenv && (fenv[0] == '0' || fenv[0] == '1');
+  if (!pinned) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      invalidate_graphs(s);
+      s->fused_xy = it->second.first;
+      s->zpers = it->second.second;
+      out4[0] = s->fused_xy;
+      out4[1] = s->zpers;
+      out4[2] = 0;
+      out4[3] = 1;
+      return CG_OK;
+    }
+  }
+  const bool fx_ok = !(fenv && fenv[0] == '0') && fused_xy_supported(s->d);
+  const int fx_lo = (fx_ok && fenv && fenv[0] == '1') ? 1 : 0;
+  const bool zp_choice = (s->d.ny % CG_ZROWS == 0) && s->d.nz != 320;
+  invalidate_graphs(s);
+  cudaEvent_t a, b;
+  CG_CUDA_TRY(cudaEventCreate(&a));
+  CG_CUDA_TRY(cudaEventCreate(&b));
+  float best = 1e30f;
+  int best_fx = 0, best_zp = 1, tried = 0;
+  for (int fx = fx_lo; fx <= (fx_ok ? 1 : 0); ++fx)
+    for (int zp = 1; zp >= (zp_choice ? 0 : 1); --zp) {
+      s->fused_xy = fx;
+      s->zpers = zp;
+      int rc = CG_OK;
+      for (int k = 0; k < 2 && rc == CG_OK; ++k) rc = launch_step(s, k % s->spp, 0);
+      CG_CUDA_TRY(cudaEventRecord(a, s->stream));
+      for (int k = 0; k < n_steps && rc == CG_OK; ++k) rc = launch_step(s, (k + 2) % s->spp, 0);
+      CG_CUDA_TRY(cudaEventRecord(b, s->stream));
+      CG_CUDA_TRY(cudaEventSynchronize(b));
+      if (rc != CG_OK) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return rc;
+      }
+      float ms = 0.f;
+      CG_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+      ++tried;
+      if (ms < best) {
+        best = ms;
+        best_fx = fx;
+        best_zp = zp;
+      }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  s->fused_xy = best_fx;
+  s->zpers = best_zp;
+  int rc = cg_solver_reset(s);
+  if (rc != CG_OK) return rc;
+  if (!pinned) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = {best_fx, best_zp};
+  }
+  out4[0] = best_fx;
+  out4[1] = best_zp;
+  out4[2] = tried;
+  out4[3] = 0;
+  return CG_OK;
 }
 
 // Per-kernel device time summed over n_steps steps (ms8[i] = launch i of

@@ -114,11 +114,12 @@ bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1
                 cudaStream_t st);
 bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float invN, float2* S0, float2* S1,
                 float2* S2, int batch, cudaStream_t st);
+// persistent = false keeps the one-tile-per-CTA z kernels (autotuner choice)
 bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
-                  int batch, cudaStream_t st);
+                  int batch, cudaStream_t st, bool persistent = true);
 bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src,
                   const RecordDev& rec, const long long* ctl, int n_local, int record, float* p, float2* S0,
-                  int batch, cudaStream_t st);
+                  int batch, cudaStream_t st, bool persistent = true);
 
 // Axis lengths with a size-specialised kernel.
 #define CG_FAST_SIZES(X) X(8) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(160) X(192) X(256)

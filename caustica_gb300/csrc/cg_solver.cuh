@@ -39,6 +39,7 @@ struct cg_solver {
   cudaStream_t stream = nullptr;
   size_t smem_y = 0, smem_x = 0, smem_z = 0;
   int fused_xy = 0;  // the transverse passes run as two cluster launches per step
+  int zpers = 1;     // persistent z-passes (where the grid allows)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one period, record off/on
   // phasors of the last finalize, [B][nh][nrec], kept for device post-processing
   float2* ph = nullptr;

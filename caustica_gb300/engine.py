@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import logging
+import os
 import time
 import warnings
 from dataclasses import dataclass, field
@@ -390,7 +391,7 @@ def device_footprint(plan: "Plan", batch: int) -> int:
 class DeviceSolver:
     """One ``cg_solver`` handle: B right-hand sides over one medium."""
 
-    def __init__(self, plan: Plan, batch: int = 1, phases: np.ndarray | None = None):
+    def __init__(self, plan: Plan, batch: int = 1, phases: np.ndarray | None = None, autotune: bool | None = None):
         self.plan = plan
         self.batch = int(batch)
         lib = _lib.load()
@@ -426,6 +427,15 @@ class DeviceSolver:
         except Exception:
             self.close()
             raise
+        self.tuning = None
+        if autotune is None:
+            autotune = os.environ.get("CG_AUTOTUNE", "1") != "0"
+        if autotune:
+            # launch configuration timed on this (fresh) handle, remembered per shape
+            out = np.zeros(4, np.int32)
+            _lib.call("cg_solver_autotune", h, 4, _lib.ptr(out))
+            self.tuning = {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]),
+                           "configurations_timed": int(out[2]), "cached": bool(out[3])}
         info = np.zeros(8, np.int64)
         _lib.call("cg_solver_info", h, _lib.ptr(info))
         self.nrec = int(info[2])

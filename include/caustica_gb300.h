@@ -113,6 +113,15 @@ int cg_solver_timed_run(cg_solver* s, int n_steps, int record, int graph, float*
 int cg_solver_profile(cg_solver* s, int n_steps, int record, float* ms8);
 /* ncell, nspec, nrec, smem y/x/z, batch, launches per step. */
 int cg_solver_info(const cg_solver* s, long long* out8);
+/* Autotuner: on a fresh handle (medium, source and drive set) time each
+ * launch configuration the grid admits -- cluster-fused or three-pass
+ * transverse chain, persistent or one-tile-per-CTA z-passes -- over
+ * n_steps steps of the handle itself, keep the fastest and reset the
+ * handle's state. The choice is remembered per (grid, batch, physics,
+ * medium storage) for the process. out4 = {fused, persistent z, configurations
+ * timed, 1 when taken from the process cache}. No counterpart in the
+ * reference (it has one code path). */
+int cg_solver_autotune(cg_solver* s, int n_steps, int* out4);
 
 /* ------------------------------------------------- batched 3-D R2C/C2R */
 

@@ -98,3 +98,21 @@ def test_fused_transverse_passes_equal_the_three_pass_chain(shape, nonlinear, mo
     (pa, ua), (pb, ub) = out
     assert np.abs(pa - pb).max() / np.abs(pb).max() < 1e-6
     assert np.abs(ua - ub).max() / np.abs(ub).max() < 1e-6
+
+
+def test_autotuner_picks_a_configuration_resets_the_state_and_caches_it(monkeypatch):
+    monkeypatch.delenv("CG_FUSED_XY", raising=False)
+    plan, grid, med, rng = _setup((96, 96, 64), True, True, seed=5)
+    with eng.DeviceSolver(plan, autotune=True) as dev:
+        t = dev.tuning
+        assert t["configurations_timed"] == 4 and not t["cached"]  # fused or not x persistent or not
+        p, u = dev.get_state()
+        assert not p.any() and not u.any()  # the trial steps left no trace
+        dev.run_steps(30)
+        pt, _ = dev.get_state()
+    with eng.DeviceSolver(plan, autotune=True) as dev:
+        assert dev.tuning["cached"] and dev.tuning["fused_transverse"] == t["fused_transverse"]
+    with eng.DeviceSolver(plan, autotune=False) as dev:  # three-pass chain, persistent z
+        dev.run_steps(30)
+        pf, _ = dev.get_state()
+    assert np.abs(pt - pf).max() / np.abs(pf).max() < 1e-5
