@@ -10,8 +10,8 @@ they exist on hosts without caustica:
   ``db_cm_to_np_m`` (materials.py:102-104).
 
 Configurations (grid, drive and medium as the benchmark definitions state
-them, with the geometry adjustments the survey measured so every source
-fits its grid):
+them, with the geometry adjusted where the stated transducer does not fit
+the stated grid):
 
 * ``config1``: linear, 96x96x128, dx 0.3 mm, 500 kHz bowl (aperture radius
   12 mm, ROC 30 mm) at apex (48, 48, 10), water, 10-cell sponge, cfl 0.3,
