@@ -225,6 +225,20 @@ struct Split {
   static constexpr bool ok = (A <= 16);
 };
 
+// Pencil split of the size-specialised passes: (A, B) with B threads
+// holding A values on input and A threads holding B values on output.
+// Lengths 16 x (<= 16) use Split<N> on 16 threads per pencil; 320 = 16 x 20
+// runs on 20 threads per pencil.
+template <int N>
+struct PSplit {
+  static constexpr int A = Split<N>::A, B = Split<N>::B;
+  static constexpr int TPP = A > B ? A : B;  // threads per pencil
+};
+template <>
+struct PSplit<320> {
+  static constexpr int A = 16, B = 20, TPP = 20;
+};
+
 // Odd leading dimension >= n (bank-conflict-free strided access).
 constexpr int ct_odd(int n) { return (n % 2) ? n : n + 1; }
 

@@ -26,26 +26,40 @@
 #endif
 
 using cgf::ColEx;
+using cgf::PSplit;
 using cgf::RowEx;
-using cgf::Split;
 using cgf::fft2;
 using cgf::static_for;
+
+// Threads and resident CTAs per SM of the y- and x-pass CTAs for length N
+// (20-thread pencils get the register budget that avoids spills).
+template <int N>
+struct YT {
+  static constexpr int TPP = PSplit<N>::TPP, THREADS = TPP * CG_YP;
+  static constexpr int MINB = TPP == 16 ? CG_FAST_MINB_Y : 4;
+};
+template <int N>
+struct XT {
+  static constexpr int TPP = PSplit<N>::TPP, THREADS = TPP * CG_XP;
+  static constexpr int MINB = TPP == 16 ? CG_FAST_MINB_X : 1;
+};
 
 // One instantiation per mode keeps each kernel's code small enough for the
 // instruction cache (the x-pass gradient loops over one copy of its inverse
 // transform; the y-pass modes stay straight-line, where the compiler hoists
 // the next input's loads above the current transform).
 template <int N, int MODE>
-__global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(Dims d, Tables t, float2* __restrict__ S0,
-                                                         float2* __restrict__ S1, float2* __restrict__ S2) {
-  constexpr int A = Split<N>::A, B = Split<N>::B;
+__global__ void __launch_bounds__(YT<N>::THREADS, YT<N>::MINB) kf_ypass(Dims d, Tables t, float2* __restrict__ S0,
+                                                                        float2* __restrict__ S1,
+                                                                        float2* __restrict__ S2) {
+  constexpr int A = PSplit<N>::A, B = PSplit<N>::B, TPP = PSplit<N>::TPP;
   using Ex = RowEx<A, B>;
   extern __shared__ float2 sm[];
   cgf::pdl_trigger();
   float2* tw = sm;  // (A, B) order
   cgf::fill_twt<A, B>(tw, t.twy);
   cgf::pdl_wait();
-  const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
+  const int s = threadIdx.x % TPP, p = threadIdx.x / TPP;
   const Ex ex{sm + N + p * Ex::SLAB};
   const long long nrows = (long long)d.nx * d.nzh;
   const long long row = (long long)blockIdx.x * CG_YP + p;
@@ -106,10 +120,11 @@ __global__ void __launch_bounds__(16 * CG_YP, CG_FAST_MINB_Y) kf_ypass(Dims d, T
 }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, Tables t, float kcoef, float invN,
-                                                         float2* __restrict__ S0, float2* __restrict__ S1,
-                                                         float2* __restrict__ S2) {
-  constexpr int A = Split<N>::A, B = Split<N>::B;
+__global__ void __launch_bounds__(XT<N>::THREADS, XT<N>::MINB) kf_xpass(Dims d, Tables t, float kcoef, float invN,
+                                                                        float2* __restrict__ S0,
+                                                                        float2* __restrict__ S1,
+                                                                        float2* __restrict__ S2) {
+  constexpr int A = PSplit<N>::A, B = PSplit<N>::B;
   extern __shared__ float2 sm[];
   cgf::pdl_trigger();
   float2* tw = sm;       // (A, B) order
@@ -205,7 +220,7 @@ __global__ void __launch_bounds__(16 * CG_XP, CG_FAST_MINB_X) kf_xpass(Dims d, T
 // twiddles | exchange | (x: a parked spectrum tile, k_x, k_x^2)
 template <int N>
 static size_t smem_y() {
-  return sizeof(float2) * (N + CG_YP * RowEx<Split<N>::A, Split<N>::B>::SLAB);
+  return sizeof(float2) * (N + CG_YP * RowEx<PSplit<N>::A, PSplit<N>::B>::SLAB);
 }
 template <int N>
 static size_t smem_x() {
@@ -219,13 +234,13 @@ bool fast_ypass(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1
 #define CASE(n)                                                                                            \
   case n:                                                                                                  \
     switch (mode) {                                                                                        \
-      case Y_FWD: cgf::launch(kf_ypass<n, Y_FWD>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break;       \
-      case Y_INV: cgf::launch(kf_ypass<n, Y_INV>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break;       \
-      case Y_INV_GRAD: cgf::launch(kf_ypass<n, Y_INV_GRAD>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break; \
-      default: cgf::launch(kf_ypass<n, Y_FWD_DIV>, grid, dim3(16 * CG_YP), smem_y<n>(), st, d, t, S0, S1, S2); break;      \
+      case Y_FWD: cgf::launch(kf_ypass<n, Y_FWD>, grid, dim3(YT<n>::THREADS), smem_y<n>(), st, d, t, S0, S1, S2); break;       \
+      case Y_INV: cgf::launch(kf_ypass<n, Y_INV>, grid, dim3(YT<n>::THREADS), smem_y<n>(), st, d, t, S0, S1, S2); break;       \
+      case Y_INV_GRAD: cgf::launch(kf_ypass<n, Y_INV_GRAD>, grid, dim3(YT<n>::THREADS), smem_y<n>(), st, d, t, S0, S1, S2); break; \
+      default: cgf::launch(kf_ypass<n, Y_FWD_DIV>, grid, dim3(YT<n>::THREADS), smem_y<n>(), st, d, t, S0, S1, S2); break;      \
     }                                                                                                      \
     return true;
-    CG_FAST_SIZES(CASE)
+    CG_FAST_XYSIZES(CASE)
 #undef CASE
     default:
       return false;
@@ -236,7 +251,7 @@ bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float inv
                 float2* S2, int batch, cudaStream_t st) {
   const dim3 grid((unsigned)(((long long)d.nzh * d.ny + CG_XP - 1) / CG_XP), batch);
   switch (d.nx) {
-#define XL(n, M) cgf::launch(kf_xpass<n, M>, grid, dim3(16 * CG_XP), smem_x<n>(), st, d, t, kcoef, invN, S0, S1, S2)
+#define XL(n, M) cgf::launch(kf_xpass<n, M>, grid, dim3(XT<n>::THREADS), smem_x<n>(), st, d, t, kcoef, invN, S0, S1, S2)
 #define CASE(n)                          \
   case n:                                \
     switch (mode) {                      \
@@ -246,7 +261,7 @@ bool fast_xpass(int mode, const Dims& d, const Tables& t, float kcoef, float inv
       default: XL(n, X_INV); break;      \
     }                                    \
     return true;
-    CG_FAST_SIZES(CASE)
+    CG_FAST_XYSIZES(CASE)
 #undef CASE
 #undef XL
     default:
@@ -266,7 +281,7 @@ int fast_prepare_yx() {
   // Y_* and X_* modes are both 0..3
 #define SET(n)                                                                                        \
   if (allow_yx<n, 0>() || allow_yx<n, 1>() || allow_yx<n, 2>() || allow_yx<n, 3>()) return -1;
-  CG_FAST_SIZES(SET)
+  CG_FAST_XYSIZES(SET)
 #undef SET
   return 0;
 }

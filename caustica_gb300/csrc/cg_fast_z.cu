@@ -22,18 +22,8 @@ using cgf::Split;
 using cgf::fft2;
 using cgf::static_for;
 
-// Pencil split of the z-transforms: (A, B) of the inverse transform (B
-// threads hold A values on input, A threads hold B values on output).
-// Lengths with a 16-point factor and a co-factor <= 16 use Split<N> on 16
-// threads per pencil; 320 = 16 x 20 runs on 20 threads per pencil.
 template <int N>
-struct ZSplit {
-  static constexpr int A = Split<N>::A, B = Split<N>::B;
-};
-template <>
-struct ZSplit<320> {
-  static constexpr int A = 16, B = 20;
-};
+using ZSplit = cgf::PSplit<N>;
 
 template <int N>
 struct ZShape {
@@ -432,7 +422,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(Dims d, T
 template <int N>
 struct ZPShape {
   static constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B, NH = N / 2 + 1;
-  static constexpr int TPP = A > B ? A : B;              // threads per pencil
+  static constexpr int TPP = ZSplit<N>::TPP;             // threads per pencil
   static constexpr int THREADS = CG_TILE * TPP;
   static constexpr int MINB = TPP == 16 ? CG_FAST_MINB : 1;  // resident CTAs per SM
   static constexpr int EX_I = RowEx<A, B>::SLAB, EX_F = RowEx<B, A>::SLAB;

@@ -123,5 +123,7 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
 
 // Axis lengths with a size-specialised kernel.
 #define CG_FAST_SIZES(X) X(8) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(160) X(192) X(256)
-// z lengths of the persistent z-passes (ny a multiple of 32): the above and 320
+// lengths of the x/y passes and of the persistent z-passes (ny a multiple of
+// 32): the above and 320 (20 threads per pencil)
 #define CG_FAST_ZSIZES(X) CG_FAST_SIZES(X) X(320)
+#define CG_FAST_XYSIZES(X) CG_FAST_SIZES(X) X(320)

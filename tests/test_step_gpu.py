@@ -18,8 +18,9 @@ CASES = [((12, 10, 16), False, True), ((9, 12, 10), True, True), ((16, 16, 24), 
          # square transverse planes: the fused cluster passes
          ((64, 64, 32), True, True), ((96, 96, 24), False, True), ((128, 128, 16), True, True),
          ((160, 160, 16), True, False), ((192, 192, 16), True, True),
-         # 320-point z on 20 threads per pencil (persistent z-passes)
-         ((16, 32, 320), True, True), ((8, 64, 320), False, True)]
+         # 320-point axes on 20 threads per pencil
+         ((16, 32, 320), True, True), ((8, 64, 320), False, True), ((320, 32, 16), True, True),
+         ((8, 320, 24), True, False)]
 FUSED = {64, 96, 128, 160, 192}
 
 
