@@ -644,6 +644,14 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   const long long Ry = rec.hi[1] - rec.lo[1], Rz = rec.hi[2] - rec.lo[2];
   const bool drive_on = src.S > 0 && n_step < src.n_drive;
   const float4 dr = drive_on ? src.drive[n_step] : make_float4(0.f, 0.f, 0.f, 0.f);
+  static_assert(B <= 32, "one mask bit per cell of a thread");
+  unsigned int zconv = 0u, zrec = 0u;  // bit b: this thread's cell z = s + A b is in the box
+  if (s < A) static_for<0, B>([&](auto bi) {
+    constexpr int b = decltype(bi)::value;
+    const int n = s + A * b;
+    if (n >= rec.clo[2] && n < rec.chi[2]) zconv |= 1u << b;
+    if (n >= rec.lo[2] && n < rec.hi[2]) zrec |= 1u << b;
+  });
   int j = 0;
   for (long long tile = t0; tile < t1; ++tile, j ^= 1) {
     const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
@@ -709,33 +717,42 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
         });
       }
     }
-    // write p, convergence peak, record window
+    // write p, convergence peak, record window (z-range membership of this
+    // thread's cells is a per-kernel bit mask, the y/x membership per tile)
     unsigned int lpeak = 0u;
     const bool x_conv = x >= rec.clo[0] && x < rec.chi[0];
     const bool x_rec = record && x >= rec.lo[0] && x < rec.hi[0];
+    const bool conv_a = x_conv && ya >= rec.clo[1] && ya < rec.chi[1];
+    const bool conv_b = x_conv && yb >= rec.clo[1] && yb < rec.chi[1];
+    const bool rec_a = x_rec && ya >= rec.lo[1] && ya < rec.hi[1];
+    const bool rec_b = x_rec && yb >= rec.lo[1] && yb < rec.hi[1];
     float* bins = rec.bins + (b_idx * rec.spp + m_bin) * rec.nrec;
     float* comp = rec.comp + (b_idx * rec.spp + m_bin) * rec.nrec;
     float* pmax = rec.pmax + b_idx * rec.nrec;
+    auto record_cell = [&](int y, int n, float pn, float apn) {
+      const long long ri = ((long long)(x - rec.lo[0]) * Ry + (y - rec.lo[1])) * Rz + (n - rec.lo[2]);
+      const float sv = bins[ri], cm0 = comp[ri];
+      const float yk = pn - cm0;
+      const float tk = sv + yk;
+      comp[ri] = (tk - sv) - yk;
+      bins[ri] = tk;
+      const float pm = pmax[ri];
+      pmax[ri] = (apn > pm || apn != apn) ? apn : pm;
+    };
     if (s < A) static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
-      for (int rr = 0; rr < 2; ++rr) {
-        const int y = rr ? yb : ya;
-        const float pn = rr ? w[b].y : w[b].x;
-        pb[(rr ? rowb : rowa) + n] = pn;
-        const float apn = fabsf(pn);
-        if (x_conv && y >= rec.clo[1] && y < rec.chi[1] && n >= rec.clo[2] && n < rec.chi[2])
-          lpeak = max(lpeak, __float_as_uint(apn));
-        if (x_rec && y >= rec.lo[1] && y < rec.hi[1] && n >= rec.lo[2] && n < rec.hi[2]) {
-          const long long ri = ((long long)(x - rec.lo[0]) * Ry + (y - rec.lo[1])) * Rz + (n - rec.lo[2]);
-          const float sv = bins[ri], cm0 = comp[ri];
-          const float yk = pn - cm0;
-          const float tk = sv + yk;
-          comp[ri] = (tk - sv) - yk;
-          bins[ri] = tk;
-          const float pm = pmax[ri];
-          pmax[ri] = (apn > pm || apn != apn) ? apn : pm;
-        }
+      const float pna = w[b].x, pnb = w[b].y;
+      pb[rowa + n] = pna;
+      pb[rowb + n] = pnb;
+      const float apa = fabsf(pna), apb = fabsf(pnb);
+      if ((zconv >> b) & 1u) {
+        if (conv_a) lpeak = max(lpeak, __float_as_uint(apa));
+        if (conv_b) lpeak = max(lpeak, __float_as_uint(apb));
+      }
+      if ((zrec >> b) & 1u) {
+        if (rec_a) record_cell(ya, n, pna, apa);
+        if (rec_b) record_cell(yb, n, pnb, apb);
       }
     });
     lpeak = __reduce_max_sync(0xffffffffu, lpeak);
