@@ -82,12 +82,24 @@ def test_an_overflowing_dose_is_caught_by_the_same_guard():
         cg.PennesSolverGB300().solve(np.full(shape, 37.0, np.float32), 2.0e6, tm, 1.0, 400, dose=True)
 
 
-@pytest.mark.parametrize("shape,boundary,tref", [((10, 9, 12), "insulated", None), ((9, 11, 8), "dirichlet", 36.0),
-                                                 ((14, 12), "dirichlet", None), ((12, 10), "insulated", 38.0)])
-def test_label_coefficients_equal_the_reference_float32_path(shape, boundary, tref):
+# The larger shapes span several tiles of the streaming label kernels (even
+# nz: z-pairs; odd nz: single cells); 40 materials exceed the 32-material
+# face table.
+@pytest.mark.parametrize("shape,boundary,tref,n_ids", [((10, 9, 12), "insulated", None, 3),
+                                                       ((9, 11, 8), "dirichlet", 36.0, 3),
+                                                       ((14, 12), "dirichlet", None, 3),
+                                                       ((12, 10), "insulated", 38.0, 3),
+                                                       ((70, 19, 40), "insulated", None, 3),
+                                                       ((40, 17, 70), "dirichlet", 36.0, 5),
+                                                       ((33, 20, 36), "dirichlet", None, 40),
+                                                       ((21, 18, 37), "dirichlet", 37.0, 4),
+                                                       ((6, 5, 2), "insulated", None, 3)])
+def test_label_coefficients_equal_the_reference_float32_path(shape, boundary, tref, n_ids):
     rng = np.random.default_rng(sum(shape))
-    ids = rng.integers(0, 3, shape)
+    ids = rng.integers(0, n_ids, shape)
     vals = {0: (0.5, 1000.0, 3600.0, 0.0), 1: (0.4, 950.0, 3400.0, 2e-3), 2: (0.55, 1050.0, 3700.0, 5e-3)}
+    for i in range(3, n_ids):
+        vals[i] = (0.3 + 0.01 * i, 900.0 + 5.0 * i, 3300.0 + 10.0 * i, 1e-4 * i)
     vols = [np.vectorize(lambda i, j=j: vals[int(i)][j])(ids).astype(np.float32) for j in range(4)]
     tm = cg.ThermalMedium(*vols, dx=0.3e-3)
     q = (rng.random(shape) ** 3 * 4e6).astype(np.float32)
