@@ -346,6 +346,8 @@ def run_gb300(args, dist, rank, ws, local):
         line["batched"] = bench_batched()
     if rank == 0 and ws == 1 and not args.skip_serving:
         line["serving"] = bench_serving()
+    if rank == 0 and ws == 1 and not args.skip_thermal:
+        line["thermal"] = bench_thermal()
     if rank == 0 and ws == 1 and not args.skip_cpu:
         cb = cpu_sample(job, target_s=float(os.environ.get("CG_CPU_SECONDS", "12")))
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -390,6 +392,48 @@ def bench_batched(n_plain: int = 4):
             "ratio": (len(res) / t_batch) * t_plain, "batched_cell_steps_per_s": len(res) * cell_steps / t_batch,
             "plain_cell_steps_per_s": cell_steps / t_plain, "plain_sample": f"{n_plain} solves",
             "timing": "wall clock of the public calls (host numpy in, host numpy out)"}
+
+
+# Pennes + CEM43 sub-step, label medium with q and dose: reads theta, label,
+# q, running maximum, dose, dose compensation (4+1+4+4+4+4 B) and writes
+# theta', maximum, dose, compensation (4x4 B) per cell.
+PENNES_BYTES_PER_CELL = 37
+
+
+def bench_thermal(shape=(256, 256, 320), seed: int = 7):
+    """The heat-up phase a served request carries (400 steps of 0.05 s, dose
+    on) on the largest serving grid, q a seeded stand-in for the acoustic
+    heating: device time of the sub-steps (CUDA events on the handle's
+    stream) and the wall clock of the public call (host numpy in and out)."""
+    import time as _t
+
+    from caustica_gb300 import workloads as wl
+    from caustica_gb300.thermal import PennesSolverGB300
+
+    th = wl.config5_thermal(shape)
+    rng = np.random.default_rng(seed)
+    q = (rng.random(shape, dtype=np.float32) * np.float32(1e5)).astype(np.float32)
+    t0 = np.full(shape, 37.0, np.float32)
+    solver = PennesSolverGB300(on_unstable="substep")
+    solver.solve(t0, q, th["medium"], dt=th["dt"], n_steps=10, dose=True)  # warm
+    timing: dict = {}
+    w0 = _t.perf_counter()
+    res = solver.solve(t0, q, th["medium"], dt=th["dt"], n_steps=th["n_heat"], dose=True, timing=timing)
+    wall = _t.perf_counter() - w0
+    cells = int(np.prod(shape))
+    n_sub = int(timing["substeps"])
+    ms_sub = timing["device_ms"] / n_sub
+    peak, kind = _peaks()
+    achieved = cells * PENNES_BYTES_PER_CELL / (ms_sub * 1e-3) / 1e9
+    return {"workload": f"pennes_cem43 {shape[0]}x{shape[1]}x{shape[2]} labels+q+dose, {th['n_heat']} steps of "
+                        f"{th['dt']} s ({res.substeps} sub-step(s) each)",
+            "kernel_symbol": "k_pennes_stream2<1, 1, 0>" if shape[2] % 2 == 0 else "k_pennes_stream<1, 1, 0>",
+            "substeps": n_sub, "ms_per_substep": ms_sub, "cell_substeps_per_s": cells / (ms_sub * 1e-3),
+            "e2e_cell_substeps_per_s": cells * n_sub / wall, "e2e_seconds": wall,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": kind, "bytes_per_cell": PENNES_BYTES_PER_CELL},
+            "timing": "device: CUDA events around each run between finite-guards (guards excluded); "
+                      "e2e: wall clock of PennesSolverGB300.solve"}
 
 
 def bench_serving(n_req: int = 16, seed: int = 5):
@@ -458,6 +502,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--skip-thermal", action="store_true")
     ap.add_argument("--prerun-periods", type=int, default=None,
                     help="periods run before the warm-up (default: the settle floor of the workload)")
     args = ap.parse_args()

@@ -722,6 +722,21 @@ extern "C" int cg_pennes_run(cg_pennes* h, int n_sub) {
   return CG_OK;
 }
 
+extern "C" int cg_pennes_timed_run(cg_pennes* h, int n_sub, float* ms) {
+  CG_REQUIRE(h && ms, "null argument");
+  cudaEvent_t a, b;
+  CG_CUDA_TRY(cudaEventCreate(&a));
+  CG_CUDA_TRY(cudaEventCreate(&b));
+  CG_CUDA_TRY(cudaEventRecord(a, h->stream));
+  const int rc = cg_pennes_run(h, n_sub);
+  CG_CUDA_TRY(cudaEventRecord(b, h->stream));
+  CG_CUDA_TRY(cudaEventSynchronize(b));
+  CG_CUDA_TRY(cudaEventElapsedTime(ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return rc;
+}
+
 extern "C" int cg_pennes_check_finite(cg_pennes* h, int* finite) {
   CG_REQUIRE(h && finite, "null argument");
   const int one = 3;

@@ -309,8 +309,13 @@ class PennesSolverGB300:
         return np.ascontiguousarray(arr), "array"
 
     def solve(self, temperature0, q, medium, dt: float, n_steps: int, *, record_every: int | None = None,
-              dose: bool = False, dose0=None) -> ThermalResult:
-        """Integrate ``n_steps`` outer steps of ``dt`` (pennes.py:451-689)."""
+              dose: bool = False, dose0=None, timing: dict | None = None) -> ThermalResult:
+        """Integrate ``n_steps`` outer steps of ``dt`` (pennes.py:451-689).
+
+        ``timing``: a dict that receives ``device_ms``, the CUDA-event time of
+        all sub-steps on the handle's stream (each run between guards is timed
+        and synchronised), and ``substeps``, their count.
+        """
         if not all(hasattr(medium, a) for a in ("k", "rho", "specific_heat", "perfusion", "dx")):
             raise TypeError(f"medium must be a ThermalMedium, got {type(medium).__name__}.")
         if not (np.isfinite(dt) and dt > 0):
@@ -447,7 +452,13 @@ class PennesSolverGB300:
                 if record_every is not None:
                     nxt = min(nxt, (step // record_every + 1) * record_every)
                 nxt = min(nxt, (step // self.finite_check_every + 1) * self.finite_check_every)
-                _lib.call("cg_pennes_run", h, (nxt - step) * n_sub)
+                if timing is None:
+                    _lib.call("cg_pennes_run", h, (nxt - step) * n_sub)
+                else:
+                    ms = C.c_float(0.0)
+                    _lib.call("cg_pennes_timed_run", h, (nxt - step) * n_sub, C.byref(ms))
+                    timing["device_ms"] = timing.get("device_ms", 0.0) + float(ms.value)
+                    timing["substeps"] = timing.get("substeps", 0) + (nxt - step) * n_sub
                 step = nxt
                 if record_every is not None and step % record_every == 0:
                     record(step)

@@ -266,6 +266,17 @@ def config5_medium(shape, dx, rng, *, nonlinear: bool):
     return Medium.from_labels(labels, table)
 
 
+def config5_thermal(shape, dx: float = 0.25e-3) -> dict:
+    """The thermal phase a served request carries: soft tissue (k 0.5 W/m/K,
+    rho 1000 kg/m^3, cp 3600 J/kg/K, perfusion 0.5/1050 1/s) on the request's
+    grid, 0.05 s steps, 400 heating then 1200 cooling, CEM43 dose on."""
+    from .thermal import ThermalMedium
+
+    return {"medium": ThermalMedium.homogeneous(tuple(shape), k=0.5, rho=1000.0, specific_heat=3600.0,
+                                                perfusion=0.5 / 1050.0, dx=dx),
+            "dt": 0.05, "n_heat": 400, "n_cool": 1200}
+
+
 def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear: float = 0.3,
                      p_thermal: float = 0.3, p_reuse: float = 0.2):
     """Seeded request stream: grid uniform over ``grids`` (dx 0.25 mm, 1 MHz,
@@ -279,7 +290,6 @@ def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear:
     Every request asks for its focal metrics (apex and geometric focus)."""
     from .metrics import FieldFrame
     from .serve import Request
-    from .thermal import ThermalMedium
 
     rng = np.random.default_rng(seed)
     dx, f0, pml = 0.25e-3, 1e6, 10
@@ -304,11 +314,7 @@ def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear:
         focus = (apex[0], apex[1], apex[2] + int(round(roc / dx)))
         spec = CWRunSpec(cfl=0.48, convergence_tol=0.0, min_settle_periods=4, max_settle_periods=4,
                          n_record_periods=2)
-        th = None
-        if thermal:
-            th = {"medium": ThermalMedium.homogeneous(shape, k=0.5, rho=1000.0, specific_heat=3600.0,
-                                                      perfusion=0.5 / 1050.0, dx=dx),
-                  "dt": 0.05, "n_heat": 400, "n_cool": 1200}
+        th = config5_thermal(shape, dx) if thermal else None
         frame = FieldFrame(dx=dx, grid_shape=shape, pml_vox=pml, apex_vox=apex, focus_vox=focus)
         reqs.append(Request(grid=grid, medium=med, source=src, spec=spec, nonlinear=nonlinear,
                             harmonics=(1, 2) if nonlinear else (1,), reference_point=focus, thermal=th, frame=frame,

@@ -194,6 +194,9 @@ int cg_pennes_set_labels(cg_pennes* h, const uint8_t* labels, int n_labels, cons
 int cg_pennes_set_state(cg_pennes* h, const float* theta, const float* theta_max, const float* dose);
 /* n_sub sub-steps (pennes.py:608-649). Async. */
 int cg_pennes_run(cg_pennes* h, int n_sub);
+/* Device time [ms] of n_sub sub-steps, CUDA events on the handle's stream.
+ * Synchronises. */
+int cg_pennes_timed_run(cg_pennes* h, int n_sub, float* ms);
 /* Bit 0 set when theta is finite everywhere, bit 1 when the dose is
  * (pennes.py:756-781). */
 int cg_pennes_check_finite(cg_pennes* h, int* finite);
