@@ -163,17 +163,19 @@ def _traffic_from_profiles(kernel: str):
 
 SLOTS = ["k_ypass:fwd", "k_xpass:grad", "k_ypass:inv_grad", "k_zpass_u", "k_ypass:fwd_div", "k_xpass:div",
          "k_ypass:inv", "k_zpass_p"]
-FAST_SIZES = {8, 16, 24, 32, 48, 64, 96, 128, 160, 192, 256}
+FAST_SIZES = {8, 16, 24, 32, 48, 64, 96, 128, 160, 192, 256}  # every size-specialised kernel family
+FAST_XYZ_SIZES = FAST_SIZES | {320, 512}  # x/y passes and the persistent z-passes only
 
 
 def slot_symbols(padded3) -> list[str]:
     """The kernel each step slot launches on this grid (size-specialised where the axis allows)."""
     nx, ny, nz = padded3
-    y = f"kf_ypass<{ny},{{}}>" if ny in FAST_SIZES else "k_ypass"
-    x = f"kf_xpass<{nx},{{}}>" if nx in FAST_SIZES else "k_xpass"
+    y = f"kf_ypass<{ny},{{}}>" if ny in FAST_XYZ_SIZES else "k_ypass"
+    x = f"kf_xpass<{nx},{{}}>" if nx in FAST_XYZ_SIZES else "k_xpass"
     zp = "kfp" if ny % 32 == 0 else "kf"
-    zu = f"{zp}_zpass_u<{nz}>" if nz in FAST_SIZES else "k_zpass_u"
-    zpp = (f"{zp}_zpass_p<{nz}>" if zp == "kfp" else f"kf_zpass_p<{nz},1>") if nz in FAST_SIZES else "k_zpass_p"
+    zfast = nz in (FAST_XYZ_SIZES if zp == "kfp" else FAST_SIZES)
+    zu = f"{zp}_zpass_u<{nz}>" if zfast else "k_zpass_u"
+    zpp = (f"{zp}_zpass_p<{nz}>" if zp == "kfp" else f"kf_zpass_p<{nz},1>") if zfast else "k_zpass_p"
     return [y.format("Y_FWD"), x.format("X_GRAD"), y.format("Y_INV_GRAD"), zu, y.format("Y_FWD_DIV"),
             x.format("X_DIV"), y.format("Y_INV"), zpp]
 

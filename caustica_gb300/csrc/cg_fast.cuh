@@ -228,7 +228,8 @@ struct Split {
 // Pencil split of the size-specialised passes: (A, B) with B threads
 // holding A values on input and A threads holding B values on output.
 // Lengths 16 x (<= 16) use Split<N> on 16 threads per pencil; 320 = 16 x 20
-// runs on 20 threads per pencil.
+// and 400 = 20 x 20 run on 20 threads per pencil, 512 = 32 x 16 (Split<512>)
+// and 640 = 32 x 20 on 32.
 template <int N>
 struct PSplit {
   static constexpr int A = Split<N>::A, B = Split<N>::B;
@@ -237,6 +238,14 @@ struct PSplit {
 template <>
 struct PSplit<320> {
   static constexpr int A = 16, B = 20, TPP = 20;
+};
+template <>
+struct PSplit<400> {
+  static constexpr int A = 20, B = 20, TPP = 20;
+};
+template <>
+struct PSplit<640> {
+  static constexpr int A = 32, B = 20, TPP = 32;
 };
 
 // Odd leading dimension >= n (bank-conflict-free strided access).

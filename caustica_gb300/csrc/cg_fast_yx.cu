@@ -285,3 +285,14 @@ int fast_prepare_yx() {
 #undef SET
   return 0;
 }
+
+bool fast_xy_has(int n) {
+  switch (n) {
+#define CASE(k) case k:
+    CG_FAST_XYSIZES(CASE)
+#undef CASE
+    return true;
+    default:
+      return false;
+  }
+}

@@ -774,7 +774,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
 bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
                   int batch, cudaStream_t st, bool persistent) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
-  if ((persistent || d.nz == 320) && d.ny % CG_ZROWS == 0) {
+  if ((persistent || !fast_has(d.nz)) && d.ny % CG_ZROWS == 0) {
     int g = 0, per = 0;
     switch (d.nz) {
 #define CASE(n)                                                                                            \
@@ -805,7 +805,7 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
                   const RecordDev& rec, const long long* ctl, int n_local, int record, float* p, float2* S0,
                   int batch, cudaStream_t st, bool persistent) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
-  if (mode == 1 && (persistent || d.nz == 320) && d.ny % CG_ZROWS == 0) {
+  if (mode == 1 && (persistent || !fast_has(d.nz)) && d.ny % CG_ZROWS == 0) {
     int g = 0, per = 0;
     switch (d.nz) {
 #define CASE(n)                                                                                               \

@@ -765,8 +765,11 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
   s->smem_y = smem_ypass(cfg->ny);
   s->smem_x = smem_xpass(cfg->nx);
   s->smem_z = smem_zpass(cfg->nz);
+  // the runtime-plan passes must fit wherever an axis has no size-specialised
+  // kernel (the runtime-plan z-pass also loads states and runs short z-rows)
   const size_t smem_max = smem_limit();
-  if (s->smem_y > smem_max || s->smem_x > smem_max || s->smem_z > smem_max) {
+  if ((!fast_xy_has(cfg->ny) && s->smem_y > smem_max) || (!fast_xy_has(cfg->nx) && s->smem_x > smem_max) ||
+      s->smem_z > smem_max) {
     cg_set_error("grid %dx%dx%d needs more than 227 KB of shared memory per tile", cfg->nx, cfg->ny, cfg->nz);
     delete s;
     return CG_ERR_INVALID;
@@ -1287,7 +1290,8 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   }
   const bool fx_ok = !(fenv && fenv[0] == '0') && fused_xy_supported(s->d);
   const int fx_lo = (fx_ok && fenv && fenv[0] == '1') ? 1 : 0;
-  const bool zp_choice = (s->d.ny % CG_ZROWS == 0) && s->d.nz != 320;
+  // the per-tile z-passes exist for the lengths of CG_FAST_SIZES only
+  const bool zp_choice = (s->d.ny % CG_ZROWS == 0) && fast_has(s->d.nz);
   invalidate_graphs(s);
   cudaEvent_t a, b;
   CG_CUDA_TRY(cudaEventCreate(&a));
@@ -1401,6 +1405,13 @@ extern "C" int cg_fft3d_create(int nx, int ny, int nz, int batch, cg_fft3d** out
   f->smem_y = smem_ypass(ny);
   f->smem_x = smem_xpass(nx);
   f->smem_z = smem_zpass(nz);
+  const size_t smem_max = smem_limit();
+  if ((!fast_xy_has(ny) && f->smem_y > smem_max) || (!fast_xy_has(nx) && f->smem_x > smem_max) ||
+      f->smem_z > smem_max) {
+    cg_set_error("FFT shape %dx%dx%d needs more than 227 KB of shared memory per tile", nx, ny, nz);
+    delete f;
+    return CG_ERR_INVALID;
+  }
   int rc;
   int mx = nx > ny ? nx : ny;
   mx = mx > nz ? mx : nz;

@@ -105,6 +105,7 @@ __device__ __forceinline__ float4 cell_coef(const MediumDev& m, long long i) {
 // Launch the size-specialised kernel for this axis length when one exists
 // (returns false otherwise; the caller then uses the generic kernel).
 bool fast_has(int n);
+bool fast_xy_has(int n);  // n in CG_FAST_XYSIZES
 int fast_prepare();  // lift the dynamic shared-memory limits (once per device)
 // fused transverse passes (cg_fused_xy.cu): 1 when they apply to the grid
 int fused_xy_supported(const Dims& d);
@@ -123,7 +124,8 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
 
 // Axis lengths with a size-specialised kernel.
 #define CG_FAST_SIZES(X) X(8) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(160) X(192) X(256)
-// lengths of the x/y passes and of the persistent z-passes (ny a multiple of
-// 32): the above and 320 (20 threads per pencil)
-#define CG_FAST_ZSIZES(X) CG_FAST_SIZES(X) X(320)
-#define CG_FAST_XYSIZES(X) CG_FAST_SIZES(X) X(320)
+// lengths of the persistent z-passes (ny a multiple of 32): the above, 320
+// and 400 (20 threads per pencil) and 512 (32 threads per pencil); of the
+// x/y passes: those and 640 (32 threads per pencil)
+#define CG_FAST_ZSIZES(X) CG_FAST_SIZES(X) X(320) X(400) X(512)
+#define CG_FAST_XYSIZES(X) CG_FAST_ZSIZES(X) X(640)

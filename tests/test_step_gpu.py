@@ -20,7 +20,13 @@ CASES = [((12, 10, 16), False, True), ((9, 12, 10), True, True), ((16, 16, 24), 
          ((160, 160, 16), True, False), ((192, 192, 16), True, True),
          # 320-point axes on 20 threads per pencil
          ((16, 32, 320), True, True), ((8, 64, 320), False, True), ((320, 32, 16), True, True),
-         ((8, 320, 24), True, False)]
+         ((8, 320, 24), True, False),
+         # 400-point axes (20 x 20) on 20 threads per pencil
+         ((16, 32, 400), True, True), ((400, 32, 16), False, True), ((8, 400, 24), True, False),
+         # 512-point axes on 32 threads per pencil
+         ((16, 32, 512), True, True), ((512, 32, 16), False, True), ((8, 512, 24), True, False),
+         # 640-point x/y axes (32 x 20) on 32 threads per pencil; z on the runtime-plan passes
+         ((640, 32, 16), True, True), ((8, 640, 24), False, True), ((8, 32, 640), True, False)]
 FUSED = {64, 96, 128, 160, 192}
 
 
