@@ -440,14 +440,16 @@ struct ZPShape {
   static constexpr size_t smem = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
 };
 
-// The half spectrum of tile (x, y0) of S into stg4[k * 17 + p], asynchronously.
+// The half spectrum of tile (x, y0) of S into stg4[k * 17 + p], asynchronously
+// (ny even; a ragged last tile stages only its rows below ny).
 template <int N>
 __device__ __forceinline__ void z_prefetch(float4* stg4, const float2* __restrict__ S, const Dims& d, int x, int y0) {
   constexpr int NH = N / 2 + 1;
   const float2* base = S + (long long)x * NH * d.ny + y0;
+  const int npp = min(CG_TILE, (d.ny - y0) >> 1);
   for (int idx = threadIdx.x; idx < NH * CG_TILE; idx += blockDim.x) {
     const int k = idx >> 4, pp = idx & 15;
-    cgf::cp_async16(stg4 + k * 17 + pp, base + (long long)k * d.ny + 2 * pp);
+    if (pp < npp) cgf::cp_async16(stg4 + k * 17 + pp, base + (long long)k * d.ny + 2 * pp);
   }
 }
 
@@ -456,7 +458,8 @@ template <int N>
 __device__ __forceinline__ void z_prefetch_labels(uint8_t* lab_s, const uint8_t* __restrict__ labels, const Dims& d,
                                                   int x, int y0) {
   const uint8_t* src = labels + ((long long)x * d.ny + y0) * N;
-  for (int i = threadIdx.x; i < CG_ZROWS * N / 16; i += blockDim.x) cgf::cp_async16(lab_s + 16 * i, src + 16 * i);
+  const int n16 = min(CG_ZROWS, d.ny - y0) * N / 16;
+  for (int i = threadIdx.x; i < n16; i += blockDim.x) cgf::cp_async16(lab_s + 16 * i, src + 16 * i);
 }
 
 // z_inputs on a raw staged tile: times i*mk[k] when mk is given, Im of the
@@ -517,7 +520,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   using Z = ZPShape<N>;
   constexpr int A = Z::A, B = Z::B;
   extern __shared__ float2 sm[];
-  const int ytiles = d.ny / CG_ZROWS;
+  const int ytiles = (d.ny + CG_ZROWS - 1) / CG_ZROWS;  // ny even; the last tile may be ragged
   const long long per_member = (long long)d.nx * ytiles;
   const long long total = per_member * n_members;
   const long long t0 = (long long)blockIdx.x * tiles_per_cta;
@@ -546,8 +549,9 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     const int ya = y0 + 2 * p, yb = ya + 1;
+    const bool va = ya < d.ny;  // this pencil's rows exist (ny even: yb too)
     const float spx = t.sx[x];
-    const float spa = spx * t.sy[ya], spb = spx * t.sy[yb];
+    const float spa = va ? spx * t.sy[ya] : 0.f, spb = va ? spx * t.sy[yb] : 0.f;
     const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
     const uint8_t* la = lab0 + ((tile - t0) & 1) * CG_ZROWS * N + (2 * p) * N;
     const uint8_t* lb = la + N;
@@ -559,8 +563,8 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       static_for<0, B>([&](auto bi) {
         constexpr int b = decltype(bi)::value;
         const int n = s + A * b;
-        ua[b] = (s < A) ? __ldg(uc + rowa + n) : 0.f;
-        ub[b] = (s < A) ? __ldg(uc + rowb + n) : 0.f;
+        ua[b] = (s < A && va) ? __ldg(uc + rowa + n) : 0.f;
+        ub[b] = (s < A && va) ? __ldg(uc + rowb + n) : 0.f;
       });
       cgf::cp_async_wait0();
       __syncthreads();
@@ -586,16 +590,18 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
         const int n = s + A * b;
         const float sz = sz_s[n];
         // (dt/rho, absorb) of the two cells
-        const float2 ca = lab ? tab2_s[la[n]] : make_float2(m.dtr[rowa + n], m.ab[rowa + n]);
-        const float2 cb = lab ? tab2_s[lb[n]] : make_float2(m.dtr[rowb + n], m.ab[rowb + n]);
+        const float2 ca = lab ? tab2_s[la[n]] : (va ? make_float2(m.dtr[rowa + n], m.ab[rowa + n]) : make_float2(0.f, 0.f));
+        const float2 cb = lab ? tab2_s[lb[n]] : (va ? make_float2(m.dtr[rowb + n], m.ab[rowb + n]) : make_float2(0.f, 0.f));
         float una = ua[b] - ca.x * w[b].x;
         una = una * ca.y;
         una = una * (spa * sz);
         float unb = ub[b] - cb.x * w[b].y;
         unb = unb * cb.y;
         unb = unb * (spb * sz);
-        uc[rowa + n] = una;
-        uc[rowb + n] = unb;
+        if (va) {
+          uc[rowa + n] = una;
+          uc[rowb + n] = unb;
+        }
         w[b] = make_float2(una, unb);
       });
       float2 X[A];
@@ -616,7 +622,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   constexpr int A = Z::A, B = Z::B;
   extern __shared__ float2 sm[];
   __shared__ unsigned int s_peak;
-  const int ytiles = d.ny / CG_ZROWS;
+  const int ytiles = (d.ny + CG_ZROWS - 1) / CG_ZROWS;  // ny even; the last tile may be ragged
   const long long per_member = (long long)d.nx * ytiles;
   const long long total = per_member * n_members;
   const long long t0 = (long long)blockIdx.x * tiles_per_cta;
@@ -657,6 +663,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     const int ya = y0 + 2 * p, yb = ya + 1;
+    const bool va = ya < d.ny;  // this pencil's rows exist (ny even: yb too)
     float* pb = p_all + b_idx * d.ncell;
     float2* S = S0 + b_idx * d.nspec;
     const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
@@ -665,8 +672,8 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
-      pa[b] = (s < A) ? __ldg(pb + rowa + n) : 0.f;
-      pbv[b] = (s < A) ? __ldg(pb + rowb + n) : 0.f;
+      pa[b] = (s < A && va) ? __ldg(pb + rowa + n) : 0.f;
+      pbv[b] = (s < A && va) ? __ldg(pb + rowb + n) : 0.f;
     });
     cgf::cp_async_wait0();
     __syncthreads();
@@ -681,14 +688,14 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const RowEx<B, A> exf{bufj + p * Z::EX};
     fft2<A, B, true>(v, w, s, sm, exi);
     const float spx = t.sx[x];
-    const float spa = spx * t.sy[ya], spb = spx * t.sy[yb];
+    const float spa = va ? spx * t.sy[ya] : 0.f, spb = va ? spx * t.sy[yb] : 0.f;
     // p <- (p - (rho c^2 dt [+ 2 beta dt p]) div u) * absorb * sponge   (engine.py:470-477)
     if (s < A) static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
       const float sz = sz_s[n];
-      const float4 ca = lab ? tab_s[la[n]] : cell_coef(m, rowa + n);
-      const float4 cb = lab ? tab_s[lb[n]] : cell_coef(m, rowb + n);
+      const float4 ca = lab ? tab_s[la[n]] : (va ? cell_coef(m, rowa + n) : make_float4(0.f, 0.f, 0.f, 0.f));
+      const float4 cb = lab ? tab_s[lb[n]] : (va ? cell_coef(m, rowb + n) : make_float4(0.f, 0.f, 0.f, 0.f));
       const float poa = pa[b], pob = pbv[b];
       float pna = m.nonlinear ? poa - (ca.y + ca.w * poa) * w[b].x : poa - ca.y * w[b].x;
       float pnb = m.nonlinear ? pob - (cb.y + cb.w * pob) * w[b].y : pob - cb.y * w[b].y;
@@ -697,7 +704,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       w[b] = make_float2(pna * (spa * sz), pnb * (spb * sz));
     });
     // source (engine.py:478-482): entries of rows ya, yb owned by this thread
-    if (drive_on && s < A) {
+    if (drive_on && s < A && va) {
       const int ra = x * d.ny + ya;
       const int e0 = src.row_ptr[ra], e1 = src.row_ptr[ra + 1], e2 = src.row_ptr[ra + 2];
       for (int e = e0; e < e2; ++e) {
@@ -720,8 +727,8 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     // write p, convergence peak, record window (z-range membership of this
     // thread's cells is a per-kernel bit mask, the y/x membership per tile)
     unsigned int lpeak = 0u;
-    const bool x_conv = x >= rec.clo[0] && x < rec.chi[0];
-    const bool x_rec = record && x >= rec.lo[0] && x < rec.hi[0];
+    const bool x_conv = va && x >= rec.clo[0] && x < rec.chi[0];
+    const bool x_rec = va && record && x >= rec.lo[0] && x < rec.hi[0];
     const bool conv_a = x_conv && ya >= rec.clo[1] && ya < rec.chi[1];
     const bool conv_b = x_conv && yb >= rec.clo[1] && yb < rec.chi[1];
     const bool rec_a = x_rec && ya >= rec.lo[1] && ya < rec.hi[1];
@@ -743,8 +750,10 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
       const float pna = w[b].x, pnb = w[b].y;
-      pb[rowa + n] = pna;
-      pb[rowb + n] = pnb;
+      if (va) {
+        pb[rowa + n] = pna;
+        pb[rowb + n] = pnb;
+      }
       const float apa = fabsf(pna), apb = fabsf(pnb);
       if ((zconv >> b) & 1u) {
         if (conv_a) lpeak = max(lpeak, __float_as_uint(apa));
@@ -774,12 +783,12 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
 bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
                   int batch, cudaStream_t st, bool persistent) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
-  if ((persistent || !fast_has(d.nz)) && d.ny % CG_ZROWS == 0) {
+  if ((persistent || !fast_has(d.nz)) && d.ny % 2 == 0) {
     int g = 0, per = 0;
     switch (d.nz) {
 #define CASE(n)                                                                                            \
   case n:                                                                                                  \
-    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, ZPShape<n>::MINB, &g, &per);         \
+    cgf::persistent_grid((long long)d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS) * batch, ZPShape<n>::MINB, &g, &per);         \
     cgf::launch(kfp_zpass_u<n>, dim3(g), dim3(ZPShape<n>::THREADS), ZPShape<n>::smem, st, d, t, m, u, S0, S1, \
                 S2, batch, per);                                                                           \
     return true;
@@ -805,12 +814,12 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
                   const RecordDev& rec, const long long* ctl, int n_local, int record, float* p, float2* S0,
                   int batch, cudaStream_t st, bool persistent) {
   const dim3 grid((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), batch);
-  if (mode == 1 && (persistent || !fast_has(d.nz)) && d.ny % CG_ZROWS == 0) {
+  if (mode == 1 && (persistent || !fast_has(d.nz)) && d.ny % 2 == 0) {
     int g = 0, per = 0;
     switch (d.nz) {
 #define CASE(n)                                                                                               \
   case n:                                                                                                     \
-    cgf::persistent_grid((long long)d.nx * (d.ny / CG_ZROWS) * batch, ZPShape<n>::MINB, &g, &per);            \
+    cgf::persistent_grid((long long)d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS) * batch, ZPShape<n>::MINB, &g, &per);            \
     cgf::launch(kfp_zpass_p<n>, dim3(g), dim3(ZPShape<n>::THREADS), ZPShape<n>::smem, st, d, t, m, src, rec,  \
                 ctl, n_local, record, p, S0, batch, per);                                                      \
     return true;

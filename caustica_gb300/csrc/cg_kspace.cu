@@ -1291,7 +1291,7 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   const bool fx_ok = !(fenv && fenv[0] == '0') && fused_xy_supported(s->d);
   const int fx_lo = (fx_ok && fenv && fenv[0] == '1') ? 1 : 0;
   // the per-tile z-passes exist for the lengths of CG_FAST_SIZES only
-  const bool zp_choice = (s->d.ny % CG_ZROWS == 0) && fast_has(s->d.nz);
+  const bool zp_choice = (s->d.ny % 2 == 0) && fast_has(s->d.nz);
   invalidate_graphs(s);
   cudaEvent_t a, b;
   CG_CUDA_TRY(cudaEventCreate(&a));
