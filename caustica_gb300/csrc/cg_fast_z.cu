@@ -430,14 +430,22 @@ struct ZPShape {
   static constexpr int B_STG = NH * 34, B_EX = CG_TILE * EX, B_XB = N * 17;  // float2 units
   static constexpr int B_MAX = B_STG > B_EX ? (B_STG > B_XB ? B_STG : B_XB) : (B_EX > B_XB ? B_EX : B_XB);
   static constexpr int BUF = (B_MAX + 1) / 2 * 2;  // even: float4-aligned
-  static constexpr int KZF = (NH + 3) / 4 * 2;     // k_z table (floats), float2 units, even
-  static constexpr int SZF = (N + 3) / 4 * 2;      // z sponge profile (floats), float2 units, even
+  // without the k_z and sponge tables: they stay in shared memory when
+  // everything fits the 227 KB a CTA may hold, else they are read through L1
+  static constexpr size_t CORE = sizeof(float2) * (2 * N + 2 * (size_t)BUF + 2 * 256) + 2 * (size_t)CG_ZROWS * N;
+  static constexpr size_t LIMIT = 232448 - 64;  // the kernels' static shared variables
+  static constexpr int KZ0 = (NH + 3) / 4 * 2, SZ0 = (N + 3) / 4 * 2;  // float2 units, even
+  static constexpr bool TBL = CORE + sizeof(float2) * (KZ0 + SZ0) <= LIMIT;
+  static constexpr int KZF = TBL ? KZ0 : 0;  // k_z table (floats), float2 units
+  static constexpr int SZF = TBL ? SZ0 : 0;  // z sponge profile (floats), float2 units
   // twiddles (two orders) | k_z | z sponge | two item buffers | material table | two label tiles
   static constexpr size_t OFF_KZ = 2 * N, OFF_SZ = OFF_KZ + KZF, OFF_BUF = OFF_SZ + SZF;
-  static constexpr size_t OFF_TAB = OFF_BUF + 2 * (size_t)BUF;  // float4 per material
-  static constexpr size_t OFF_TAB2 = OFF_TAB + 2 * 256;          // float2 (dt/rho, absorb) per material
-  static constexpr size_t OFF_LAB = OFF_TAB2 + 256;
+  // per material: float4 (k-space p coefficients) in the p-pass, float2
+  // (dt/rho, absorb) in the u-pass, in the same place
+  static constexpr size_t OFF_TAB = OFF_BUF + 2 * (size_t)BUF;
+  static constexpr size_t OFF_LAB = OFF_TAB + 2 * 256;
   static constexpr size_t smem = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
+  static_assert(smem <= LIMIT, "persistent z-pass tile does not fit shared memory");
 };
 
 // The half spectrum of tile (x, y0) of S into stg4[k * 17 + p], asynchronously
@@ -493,22 +501,24 @@ __device__ __forceinline__ void z_inputs_raw(float2 (&v)[ZSplit<N>::A], const fl
   });
 }
 
-template <int N>
+template <int N, bool UPASS>
 __device__ __forceinline__ void zp_tables(float2* sm, const Tables& t, const MediumDev& m) {
   using Z = ZPShape<N>;
   cgf::fill_twt<Z::A, Z::B>(sm, t.twz);
   cgf::fill_twt<Z::B, Z::A>(sm + N, t.twz);
-  float* kz_s = reinterpret_cast<float*>(sm + Z::OFF_KZ);
-  for (int i = threadIdx.x; i < Z::NH; i += blockDim.x) kz_s[i] = t.kz[i];
-  float* sz_s = reinterpret_cast<float*>(sm + Z::OFF_SZ);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) sz_s[i] = t.sz[i];
-  float4* tab_s = reinterpret_cast<float4*>(sm + Z::OFF_TAB);
-  float2* tab2_s = sm + Z::OFF_TAB2;
+  if (Z::TBL) {
+    float* kz_s = reinterpret_cast<float*>(sm + Z::OFF_KZ);
+    for (int i = threadIdx.x; i < Z::NH; i += blockDim.x) kz_s[i] = t.kz[i];
+    float* sz_s = reinterpret_cast<float*>(sm + Z::OFF_SZ);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) sz_s[i] = t.sz[i];
+  }
   if (m.labels)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
       const float4 c = m.ltab[i];
-      tab_s[i] = c;
-      tab2_s[i] = make_float2(c.x, c.z);
+      if (UPASS)
+        sm[Z::OFF_TAB + i] = make_float2(c.x, c.z);
+      else
+        reinterpret_cast<float4*>(sm + Z::OFF_TAB)[i] = c;
     }
 }
 
@@ -527,11 +537,11 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   const long long t1 = min(total, t0 + tiles_per_cta);
   cgf::pdl_trigger();
   if (t0 >= t1) return;  // the whole CTA, before any barrier
-  zp_tables<N>(sm, t, m);
+  zp_tables<N, true>(sm, t, m);
   cgf::pdl_wait();
-  const float* kz_s = reinterpret_cast<const float*>(sm + Z::OFF_KZ);
-  const float* sz_s = reinterpret_cast<const float*>(sm + Z::OFF_SZ);
-  const float2* tab2_s = sm + Z::OFF_TAB2;
+  const float* kz_s = Z::TBL ? reinterpret_cast<const float*>(sm + Z::OFF_KZ) : t.kz;
+  const float* sz_s = Z::TBL ? reinterpret_cast<const float*>(sm + Z::OFF_SZ) : t.sz;
+  const float2* tab2_s = sm + Z::OFF_TAB;
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
   const int s = threadIdx.x % Z::TPP, p = threadIdx.x / Z::TPP;
@@ -629,10 +639,10 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   const long long t1 = min(total, t0 + tiles_per_cta);
   cgf::pdl_trigger();
   if (t0 >= t1) return;  // the whole CTA, before any barrier
-  zp_tables<N>(sm, t, m);
+  zp_tables<N, false>(sm, t, m);
   cgf::pdl_wait();
   if (threadIdx.x == 0) s_peak = 0u;
-  const float* sz_s = reinterpret_cast<const float*>(sm + Z::OFF_SZ);
+  const float* sz_s = Z::TBL ? reinterpret_cast<const float*>(sm + Z::OFF_SZ) : t.sz;
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;

@@ -124,8 +124,8 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
 
 // Axis lengths with a size-specialised kernel.
 #define CG_FAST_SIZES(X) X(8) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(160) X(192) X(256)
-// lengths of the persistent z-passes (ny a multiple of 32): the above, 320
-// and 400 (20 threads per pencil) and 512 (32 threads per pencil); of the
-// x/y passes: those and 640 (32 threads per pencil)
-#define CG_FAST_ZSIZES(X) CG_FAST_SIZES(X) X(320) X(400) X(512)
-#define CG_FAST_XYSIZES(X) CG_FAST_ZSIZES(X) X(640)
+// lengths of the x/y passes and of the persistent z-passes (ny even): the
+// above, 320 and 400 (20 threads per pencil), 512 and 640 (32 threads per
+// pencil)
+#define CG_FAST_ZSIZES(X) CG_FAST_SIZES(X) X(320) X(400) X(512) X(640)
+#define CG_FAST_XYSIZES(X) CG_FAST_ZSIZES(X)

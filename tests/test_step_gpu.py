@@ -25,8 +25,9 @@ CASES = [((12, 10, 16), False, True), ((9, 12, 10), True, True), ((16, 16, 24), 
          ((16, 32, 400), True, True), ((400, 32, 16), False, True), ((8, 400, 24), True, False),
          # 512-point axes on 32 threads per pencil
          ((16, 32, 512), True, True), ((512, 32, 16), False, True), ((8, 512, 24), True, False),
-         # 640-point x/y axes (32 x 20) on 32 threads per pencil; z on the runtime-plan passes
+         # 640-point axes (32 x 20) on 32 threads per pencil
          ((640, 32, 16), True, True), ((8, 640, 24), False, True), ((8, 32, 640), True, False),
+         ((6, 34, 640), False, True),
          # persistent z-passes with a ragged last y-tile (ny even, not a multiple of 32)
          ((6, 40, 400), True, True), ((4, 18, 512), False, True), ((5, 34, 320), True, False)]
 FUSED = {64, 96, 128, 160, 192}
