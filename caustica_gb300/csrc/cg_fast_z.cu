@@ -425,6 +425,9 @@ struct ZPShape {
   static constexpr int TPP = ZSplit<N>::TPP;             // threads per pencil
   static constexpr int THREADS = CG_TILE * TPP;
   static constexpr int MINB = TPP == 16 ? CG_FAST_MINB : 1;  // resident CTAs per SM
+  // the field values of a thread load before its inverse transform unless
+  // the transform's A values per thread leave no registers for them
+  static constexpr bool EARLY = A <= 20;
   static constexpr int EX_I = RowEx<A, B>::SLAB, EX_F = RowEx<B, A>::SLAB;
   static constexpr int EX = EX_I > EX_F ? EX_I : EX_F;
   static constexpr int B_STG = NH * 34, B_EX = CG_TILE * EX, B_XB = N * 17;  // float2 units
@@ -569,13 +572,17 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     for (int comp = 0; comp < 3; ++comp, j ^= 1) {
       float* uc = u + ((long long)comp * n_members + b_idx) * d.ncell;
       // this thread's velocities load while the staged spectrum is transformed
+      // (after it where A-value registers would not leave room for them)
       float ua[B], ub[B];
-      static_for<0, B>([&](auto bi) {
-        constexpr int b = decltype(bi)::value;
-        const int n = s + A * b;
-        ua[b] = (s < A && va) ? __ldg(uc + rowa + n) : 0.f;
-        ub[b] = (s < A && va) ? __ldg(uc + rowb + n) : 0.f;
-      });
+      auto load_u = [&]() {
+        static_for<0, B>([&](auto bi) {
+          constexpr int b = decltype(bi)::value;
+          const int n = s + A * b;
+          ua[b] = (s < A && va) ? __ldg(uc + rowa + n) : 0.f;
+          ub[b] = (s < A && va) ? __ldg(uc + rowb + n) : 0.f;
+        });
+      };
+      if (Z::EARLY) load_u();
       cgf::cp_async_wait0();
       __syncthreads();
       {
@@ -594,6 +601,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       const RowEx<A, B> exi{bufj + p * Z::EX};
       const RowEx<B, A> exf{bufj + p * Z::EX};
       fft2<A, B, true>(v, w, s, sm, exi);
+      if (!Z::EARLY) load_u();
       // u <- (u - dt/rho g) * absorb * sponge   (engine.py:462-464)
       if (s < A) static_for<0, B>([&](auto bi) {
         constexpr int b = decltype(bi)::value;
@@ -678,13 +686,17 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     float2* S = S0 + b_idx * d.nspec;
     const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
     // this thread's pressures load while the staged spectrum is transformed
+    // (after it where A-value registers would not leave room for them)
     float pa[B], pbv[B];
-    static_for<0, B>([&](auto bi) {
-      constexpr int b = decltype(bi)::value;
-      const int n = s + A * b;
-      pa[b] = (s < A && va) ? __ldg(pb + rowa + n) : 0.f;
-      pbv[b] = (s < A && va) ? __ldg(pb + rowb + n) : 0.f;
-    });
+    auto load_p = [&]() {
+      static_for<0, B>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        const int n = s + A * b;
+        pa[b] = (s < A && va) ? __ldg(pb + rowa + n) : 0.f;
+        pbv[b] = (s < A && va) ? __ldg(pb + rowb + n) : 0.f;
+      });
+    };
+    if (Z::EARLY) load_p();
     cgf::cp_async_wait0();
     __syncthreads();
     if (tile + 1 < t1) prefetch(tile + 1, j ^ 1);
@@ -697,6 +709,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const RowEx<A, B> exi{bufj + p * Z::EX};
     const RowEx<B, A> exf{bufj + p * Z::EX};
     fft2<A, B, true>(v, w, s, sm, exi);
+    if (!Z::EARLY) load_p();
     const float spx = t.sx[x];
     const float spa = va ? spx * t.sy[ya] : 0.f, spb = va ? spx * t.sy[yb] : 0.f;
     // p <- (p - (rho c^2 dt [+ 2 beta dt p]) div u) * absorb * sponge   (engine.py:470-477)
