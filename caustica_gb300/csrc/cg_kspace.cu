@@ -1432,11 +1432,6 @@ extern "C" int cg_fft3d_create(int nx, int ny, int nz, int batch, cg_fft3d** out
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_xpass);
   if (e == cudaSuccess) e = allow_max_smem((const void*)k_zpass_p);
   if (e == cudaSuccess && fast_prepare() != 0) e = cudaErrorInvalidValue;
-  if (e == cudaSuccess && (f->smem_y > smem_limit() || f->smem_x > smem_limit() || f->smem_z > smem_limit())) {
-    cg_set_error("FFT shape %dx%dx%d needs more shared memory per tile than the device offers", nx, ny, nz);
-    fft_free(f);
-    return CG_ERR_INVALID;
-  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
   if (e != cudaSuccess) {
     cg_set_error("fft set-up: %s", cudaGetErrorString(e));
@@ -1567,7 +1562,7 @@ extern "C" int cg_fft3d_forward_noalloc(int nx, int ny, int nz, int batch, const
     return CG_ERR_INVALID;
   }
   const size_t sy = smem_ypass(ny), sx = smem_xpass(nx), sz = smem_zpass(nz), lim = smem_limit();
-  CG_REQUIRE(sy <= lim && sx <= lim && sz <= lim,
+  CG_REQUIRE((fast_xy_has(ny) || sy <= lim) && (fast_xy_has(nx) || sx <= lim) && sz <= lim,
              "FFT shape %dx%dx%d needs more shared memory per tile than the device offers", nx, ny, nz);
   int dev = 0;
   CG_CUDA_TRY(cudaGetDevice(&dev));

@@ -14,7 +14,9 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(8, 8, 8), (8, 9, 6), (6, 6, 8), (9, 8, 8), (1, 1, 600), (1, 20, 24), (16, 24, 30), (5, 12, 10),
           (3, 25, 9), (96, 96, 128), (40, 48, 64), (64, 80, 96), (20, 24, 320),
           # every axis on the size-specialised path
-          (16, 24, 32), (32, 48, 48), (8, 16, 256), (160, 16, 8), (24, 192, 16), (128, 64, 24)]
+          (16, 24, 32), (32, 48, 48), (8, 16, 256), (160, 16, 8), (24, 192, 16), (128, 64, 24),
+          # x/y passes on the 20- and 32-thread pencil splits (z on the runtime-plan passes here)
+          (320, 8, 6), (6, 400, 8), (512, 6, 4), (4, 640, 6), (8, 4, 400), (4, 6, 512), (4, 8, 640)]
 
 
 def _rel(a, b):
