@@ -556,6 +556,9 @@ extern "C" int cg_pennes_create(const cg_pennes_config* cfg, cg_pennes** out) {
   CG_REQUIRE(cfg && out, "null argument");
   *out = nullptr;
   CG_REQUIRE(cfg->nx >= 1 && cfg->ny >= 1 && cfg->nz >= 1, "invalid thermal grid %dx%dx%d", cfg->nx, cfg->ny, cfg->nz);
+  // the streaming kernels address a cell inside its x plane with 32-bit offsets
+  CG_REQUIRE((long long)cfg->ny * cfg->nz < (1LL << 31), "thermal grid %dx%dx%d: an x plane (ny x nz) must hold "
+             "fewer than 2^31 cells", cfg->nx, cfg->ny, cfg->nz);
   cg_pennes* h = new cg_pennes();
   h->cfg = *cfg;
   const long long nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
