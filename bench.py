@@ -307,6 +307,7 @@ def run_gb300(args, dist, rank, ws, local):
     traffic = _traffic_from_profiles(kernel_name)
     step_b = step_algorithmic_bytes(info_labels, True)
     step_achieved = step_b * value / ws / 1e9
+    passes_achieved = sum(bytes_slot) / (t_ms / K * 1e-3) / 1e9
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": t_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -325,6 +326,10 @@ def run_gb300(args, dist, rank, ws, local):
             "step_roofline": {"bytes_per_cell_step": step_b, "achieved": step_achieved, "peak": hbm,
                               "frac": step_achieved / hbm, "unit": "GB/s",
                               "note": "algorithmic bytes of the fully fused step with label-indexed maps"},
+            "passes_roofline": {"bytes_per_step": int(sum(bytes_slot)), "achieved": passes_achieved, "peak": hbm,
+                                "frac": passes_achieved / hbm, "unit": "GB/s",
+                                "note": "algorithmic bytes of the 8 passes as built (each input read and output "
+                                        "written once per pass) over the graph-timed step"},
             "profile_ms_per_launch": {SLOTS[i]: float(per_launch_ms[i]) for i in range(8)},
             "gpu_launches": K * launches_per_step + (K // plan.spp if graph else 1)}
 
