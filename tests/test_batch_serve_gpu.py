@@ -49,8 +49,11 @@ def _solo(grid, med, idx, ph, spec, nonlinear, harmonics=(1,)):
     return s.run(grid, med, src, spec, harmonics=harmonics)
 
 
-def test_steering_batch_members_equal_their_solo_solves():
-    grid, med, idx, rng = _setup((16, 24, 32), 1)
+# the larger z axes run the persistent z-passes on 20- and 32-thread pencils
+# with a ragged last y-tile, for every member of the batch
+@pytest.mark.parametrize("shape", [(16, 24, 32), (12, 40, 400), (8, 34, 640)])
+def test_steering_batch_members_equal_their_solo_solves(shape):
+    grid, med, idx, rng = _setup(shape, 1)
     phases = rng.uniform(0, 2 * np.pi, (5, len(idx))).astype(np.float32)
     spec = cg.CWRunSpec(convergence_tol=0.0, min_settle_periods=2, max_settle_periods=3, n_record_periods=2)
     res = solve_steering(grid, med, idx, phases, f0=1e6, amplitude=2e5, spec=spec)
