@@ -143,10 +143,11 @@ __device__ __forceinline__ void pennes_cell(const PennesDev& P, const float* __r
   }
 }
 
-// One sub-step. Block (32, PENNES_ROWS): each warp walks one (x, y) row along
-// z, so accesses along z are coalesced and the coordinates need no 64-bit
-// division; the rows of a block are consecutive in y, so the y-neighbours of
-// most cells are already in L1.
+// One sub-step on dense per-cell coefficient maps (label media take the
+// streaming kernels below). Block (32, PENNES_ROWS): each warp walks one
+// (x, y) row along z, so accesses along z are coalesced and the coordinates
+// need no 64-bit division; the rows of a block are consecutive in y, so the
+// y-neighbours of most cells are already in L1.
 #define PENNES_ROWS 8
 __global__ void __launch_bounds__(32 * PENNES_ROWS) k_pennes_step(PennesDev P, const float* __restrict__ th,
                                                                   float* __restrict__ thn, float* thmax, float* dose,
