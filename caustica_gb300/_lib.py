@@ -123,6 +123,8 @@ SIGNATURES = {
     "cg_pennes_set_state": [_P, _P, _P, _P],
     "cg_pennes_run": [_P, _I],
     "cg_pennes_timed_run": [_P, _I, _P],
+    "cg_pennes_set_temperature": [_P, _P, _P, _P],
+    "cg_pennes_get_temperature": [_P, _P, _P, _P],
     "cg_pennes_check_finite": [_P, _P],
     "cg_pennes_get_state": [_P, _P, _P, _P],
     "cg_focus_metrics": [C.POINTER(FocusInput), C.POINTER(FocusReport), _P],

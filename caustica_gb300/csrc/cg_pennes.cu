@@ -665,6 +665,40 @@ extern "C" int cg_pennes_set_state(cg_pennes* h, const float* theta, const float
   return CG_OK;
 }
 
+// dst = src + off (float32, round to nearest; off = -t_ref gives the host's
+// float32 T - t_ref bit for bit, off = +t_ref its theta + t_ref); dst2 gets a copy.
+__global__ void k_pennes_offset(const float* __restrict__ src, float* __restrict__ dst, float* __restrict__ dst2,
+                                long long n, float off) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float v = __fadd_rn(src[i], off);
+    dst[i] = v;
+    if (dst2) dst2[i] = v;
+  }
+}
+
+extern "C" int cg_pennes_set_temperature(cg_pennes* h, const float* T, const float* dose, int* finite) {
+  CG_REQUIRE(h && T && finite, "null argument");
+  const size_t n = (size_t)h->ncell;
+  h->cur = 0;
+  // T lands in the second state buffer, theta = T - t_ref in the first and in theta_max
+  CG_CUDA_TRY(cudaMemcpyAsync(h->th[1], T, 4 * n, cudaMemcpyDefault, h->stream));
+  k_pennes_offset<<<2048, 256, 0, h->stream>>>(h->th[1], h->th[0], h->thmax, h->ncell, -h->cfg.t_ref);
+  CG_CUDA_TRY(cudaGetLastError());
+  if (dose) CG_CUDA_TRY(cudaMemcpyAsync(h->dose, dose, 4 * n, cudaMemcpyDefault, h->stream));
+  else CG_CUDA_TRY(cudaMemsetAsync(h->dose, 0, 4 * n, h->stream));
+  CG_CUDA_TRY(cudaMemsetAsync(h->dcomp, 0, 4 * n, h->stream));
+  const int all = 3;
+  CG_CUDA_TRY(cudaMemcpyAsync(h->flag, &all, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  k_pennes_finite<<<1024, 256, 0, h->stream>>>(h->th[0], nullptr, h->ncell, h->flag);
+  CG_CUDA_TRY(cudaGetLastError());
+  int v = 0;
+  CG_CUDA_TRY(cudaMemcpyAsync(&v, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  *finite = v & 1;
+  h->has_state = 1;
+  return CG_OK;
+}
+
 static PennesDev make_dev(const cg_pennes* h) {
   PennesDev P;
   P.nx = h->cfg.nx; P.ny = h->cfg.ny; P.nz = h->cfg.nz;
@@ -751,6 +785,25 @@ extern "C" int cg_pennes_check_finite(cg_pennes* h, int* finite) {
   CG_CUDA_TRY(cudaMemcpyAsync(&v, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CG_CUDA_TRY(cudaStreamSynchronize(h->stream));
   *finite = v;
+  return CG_OK;
+}
+
+extern "C" int cg_pennes_get_temperature(cg_pennes* h, float* T, float* T_max, float* dose) {
+  CG_REQUIRE(h, "null handle");
+  const size_t n = (size_t)h->ncell;
+  float* scratch = h->th[1 - h->cur];  // rewritten in full by the next sub-step
+  if (T) {
+    k_pennes_offset<<<2048, 256, 0, h->stream>>>(h->th[h->cur], scratch, nullptr, h->ncell, h->cfg.t_ref);
+    CG_CUDA_TRY(cudaGetLastError());
+    CG_CUDA_TRY(cudaMemcpyAsync(T, scratch, 4 * n, cudaMemcpyDefault, h->stream));
+  }
+  if (T_max) {
+    k_pennes_offset<<<2048, 256, 0, h->stream>>>(h->thmax, scratch, nullptr, h->ncell, h->cfg.t_ref);
+    CG_CUDA_TRY(cudaGetLastError());
+    CG_CUDA_TRY(cudaMemcpyAsync(T_max, scratch, 4 * n, cudaMemcpyDefault, h->stream));
+  }
+  if (dose) CG_CUDA_TRY(cudaMemcpyAsync(dose, h->dose, 4 * n, cudaMemcpyDefault, h->stream));
+  CG_CUDA_TRY(cudaStreamSynchronize(h->stream));
   return CG_OK;
 }
 

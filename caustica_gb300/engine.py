@@ -127,6 +127,28 @@ def _first_occurrence(inv: np.ndarray, n: int, chunk: int = 1 << 20) -> np.ndarr
     return first
 
 
+def _uniform(flat) -> bool:
+    """Every volume bitwise equal to its own first value, checked in chunks on
+    a few host threads (the NumPy compares release the GIL)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    bits = [f.view(np.uint32) for f in flat]
+    first = [b[0] for b in bits]
+    n = bits[0].size
+    nt = max(1, min(8, os.cpu_count() or 1))
+    step = max(1 << 18, (n + 4 * nt - 1) // (4 * nt))
+
+    def chunk(a):
+        b = min(n, a + step)
+        return all(not np.any(x[a:b] != v) for x, v in zip(bits, first))
+
+    if n <= step:
+        return chunk(0)
+    with ThreadPoolExecutor(nt) as ex:
+        return all(ex.map(chunk, range(0, n, step)))
+
+
 def _labels_match(props: np.ndarray, inv: np.ndarray, vols) -> bool:
     """props[inv] == vols bit for bit, checked in chunks on a few host threads
     (the NumPy gathers and compares release the GIL)."""
@@ -183,7 +205,7 @@ def label_volumes(vols, id_map=None, max_labels: int = 256):
                     if _labels_match(props, inv, vols):
                         return inv.reshape(vols[0].shape), props
     flat = [v.reshape(-1) for v in vols]
-    if all(np.all(f == f[0]) for f in flat):
+    if _uniform(flat):
         return (np.zeros(vols[0].shape, np.uint8),
                 np.array([[f[0] for f in flat]], np.float32))
     bits = [f.view(np.uint32).astype(np.uint64) for f in flat]

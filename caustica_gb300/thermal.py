@@ -335,20 +335,25 @@ class PennesSolverGB300:
             raise ValueError(f"temperature0 has shape {tuple(np.shape(temperature0))} but the thermal medium is "
                              f"{shape}.")
         t_ref = np.float32(self.reference_temperature_c)
-        theta = np.asarray(temperature0, np.float32) - t_ref
-        if not bool(np.isfinite(theta).all()):
-            raise ValueError("temperature0 contains non-finite values; a solve cannot start from a field that is "
-                             "not a temperature.")
+        # theta = T0 - t_ref, its finiteness check (pennes.py:531-536) and
+        # T = theta + t_ref on the way out run on the device
+        temp0 = np.ascontiguousarray(temperature0, dtype=np.float32)
         q_arr, q_kind = self._prepare_q(q, medium)
-        perfused = bool(medium.is_perfused)
         ref_minus_ta = np.float32(self.reference_temperature_c - self.arterial_temperature_c)
         theta_wall = np.float32(self.boundary_temperature_c) - t_ref
         lab = thermal_labels(medium)
         if lab is not None:
             # per-material coefficients with the reference's float32 arithmetic
             lab_vol, props = lab
+            perfused = bool((props[:, 3] > 0).any())
             pm = ThermalMedium(props[:, 0], props[:, 1], props[:, 2], props[:, 3], dx=medium.dx)
-            dt_stable = self.stable_dt(medium)
+            if len(props) == 1:
+                # one material: the bound of its min(n, 3)-cell representative is the grid's
+                rep = tuple(min(n, 3) for n in shape)
+                dt_stable = self.stable_dt(ThermalMedium(*(np.full(rep, props[0, j], np.float32) for j in range(4)),
+                                                         dx=medium.dx))
+            else:
+                dt_stable = self.stable_dt(medium)
             n_sub = self._resolve_substeps(dt, dt_stable, medium)
             dt_sub = dt / n_sub
             perf_l = self._perf(pm)
@@ -359,6 +364,7 @@ class PennesSolverGB300:
                                                    poff_l], axis=1).astype(np.float32))
             faces = walls = perf = coeff = perf_offset = None
         else:
+            perfused = bool(medium.is_perfused)
             k = np.asarray(medium.k, np.float32)
             faces = self._faces(k, medium.dx)
             walls = self._walls(k, medium.dx) if self.boundary == "dirichlet" else None
@@ -418,14 +424,17 @@ class PennesSolverGB300:
                           _lib.ptr(wall_buf), _lib.ptr(np.ascontiguousarray(perf)) if perfused else None,
                           _lib.ptr(np.ascontiguousarray(coeff)), _qptr(q_arr),
                           _lib.ptr(np.ascontiguousarray(perf_offset)) if perf_offset is not None else None)
-            theta = np.ascontiguousarray(theta, np.float32)
-            _lib.call("cg_pennes_set_state", h, _lib.ptr(theta), _lib.ptr(theta), _lib.ptr(dose_arr))
+            fin = C.c_int(0)
+            _lib.call("cg_pennes_set_temperature", h, _lib.ptr(temp0), _lib.ptr(dose_arr), C.byref(fin))
+            if not fin.value:
+                raise ValueError("temperature0 contains non-finite values; a solve cannot start from a field that "
+                                 "is not a temperature.")
             samples, times = [], []
             buf = np.empty(shape, np.float32)
 
             def record(step_idx):
-                _lib.call("cg_pennes_get_state", h, _lib.ptr(buf), None, None)
-                samples.append(buf.copy() + t_ref)
+                _lib.call("cg_pennes_get_temperature", h, _lib.ptr(buf), None, None)
+                samples.append(buf.copy())
                 times.append(step_idx * dt)
 
             def guard(step):
@@ -470,11 +479,11 @@ class PennesSolverGB300:
             T = np.empty(shape, np.float32)
             Tm = np.empty(shape, np.float32)
             D = np.empty(shape, np.float32) if dose else None
-            _lib.call("cg_pennes_get_state", h, _lib.ptr(T), _lib.ptr(Tm), _lib.ptr(D))
+            _lib.call("cg_pennes_get_temperature", h, _lib.ptr(T), _lib.ptr(Tm), _lib.ptr(D))
         finally:
             lib.cg_pennes_destroy(h)
         return ThermalResult(
-            temperature=T + t_ref, temperature_max=Tm + t_ref, dose_cem43=D, samples=samples, times=times,
+            temperature=T, temperature_max=Tm, dose_cem43=D, samples=samples, times=times,
             dt=float(dt), n_steps=n_steps, t_end_s=float(dt * n_steps), substeps=n_sub,
             meta={"scheme": SCHEME, "backend": "gb300", "boundary": self.boundary,
                   "boundary_temperature_c": self.boundary_temperature_c, "dt_stable_s": dt_stable,

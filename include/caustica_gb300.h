@@ -192,6 +192,11 @@ int cg_pennes_set_labels(cg_pennes* h, const uint8_t* labels, int n_labels, cons
 /* State (host or device): theta = T - t_ref, theta_max, dose, and the
  * dose-rate carry; dose/dose_comp may be NULL when dose is off. */
 int cg_pennes_set_state(cg_pennes* h, const float* theta, const float* theta_max, const float* dose);
+/* State from temperatures T [cells] (host or device): theta = T - t_ref and
+ * theta_max = theta, formed on the device in float32 with round to nearest
+ * (the host's float32 subtraction bit for bit); dose NULL = zero. *finite = 1
+ * when every theta is finite (pennes.py:531-536). */
+int cg_pennes_set_temperature(cg_pennes* h, const float* T, const float* dose, int* finite);
 /* n_sub sub-steps (pennes.py:608-649). Async. */
 int cg_pennes_run(cg_pennes* h, int n_sub);
 /* Device time [ms] of n_sub sub-steps, CUDA events on the handle's stream.
@@ -201,6 +206,9 @@ int cg_pennes_timed_run(cg_pennes* h, int n_sub, float* ms);
  * (pennes.py:756-781). */
 int cg_pennes_check_finite(cg_pennes* h, int* finite);
 int cg_pennes_get_state(cg_pennes* h, float* theta, float* theta_max, float* dose);
+/* T = theta + t_ref, T_max = theta_max + t_ref (float32 on the device) and the
+ * dose; any output may be NULL. */
+int cg_pennes_get_temperature(cg_pennes* h, float* T, float* T_max, float* dose);
 
 /* ------------------------------------------ post-processing on the device */
 

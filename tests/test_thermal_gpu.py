@@ -64,6 +64,16 @@ def test_cem43_unit_definitions_on_the_device():
         np.testing.assert_allclose(res.dose_cem43, want, rtol=1e-6)
 
 
+def test_a_non_finite_initial_temperature_is_refused():
+    """pennes.py:531-536, checked on the device after the upload."""
+    shape = (6, 7, 8)
+    tm = cg.ThermalMedium.homogeneous(shape, k=0.5, rho=1050.0, specific_heat=3600.0, perfusion=0.0, dx=1e-3)
+    t0 = np.full(shape, 37.0, np.float32)
+    t0[3, 4, 5] = np.nan
+    with pytest.raises(ValueError, match="temperature0 contains non-finite values"):
+        cg.PennesSolverGB300().solve(t0, None, tm, 0.01, 2)
+
+
 def test_a_state_that_stops_being_finite_raises_instead_of_returning_nan():
     """A near-insulator with a heat source float32 cannot carry (the reference's own recipe)."""
     shape = (8, 8, 8)
