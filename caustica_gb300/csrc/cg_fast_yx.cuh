@@ -22,6 +22,11 @@
 #ifndef CG_FAST_MINB_X
 #define CG_FAST_MINB_X 3
 #endif
+// the same for the x-pass modes other than X_DIV (the divergence pass parks
+// a spectrum tile and needs the larger register budget)
+#ifndef CG_FAST_MINB_XG
+#define CG_FAST_MINB_XG CG_FAST_MINB_X
+#endif
 // rows per y-CTA and columns per x-CTA (16 threads each)
 #ifndef CG_YP
 #define CG_YP 4
@@ -47,6 +52,7 @@ template <int N>
 struct XT {
   static constexpr int TPP = PSplit<N>::TPP, THREADS = TPP * CG_XP;
   static constexpr int MINB = TPP == 16 ? CG_FAST_MINB_X : 1;
+  static constexpr int minb(int mode) { return TPP == 16 && mode != X_DIV ? CG_FAST_MINB_XG : MINB; }
 };
 
 // One instantiation per mode keeps each kernel's code small enough for the
@@ -125,7 +131,7 @@ __global__ void __launch_bounds__(YT<N>::THREADS, YT<N>::MINB) kf_ypass(Dims d, 
 }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(XT<N>::THREADS, XT<N>::MINB) kf_xpass(Dims d, Tables t, float kcoef, float invN,
+__global__ void __launch_bounds__(XT<N>::THREADS, XT<N>::minb(MODE)) kf_xpass(Dims d, Tables t, float kcoef, float invN,
                                                                         float2* __restrict__ S0,
                                                                         float2* __restrict__ S1,
                                                                         float2* __restrict__ S2) {
