@@ -27,6 +27,12 @@
 #ifndef CG_FAST_MINB_XG
 #define CG_FAST_MINB_XG CG_FAST_MINB_X
 #endif
+// and for those modes on the 320-point x axis (20-thread pencils: two CTAs
+// per SM measured 1408 -> 1365 us per 320^3 step; the 400-point axis keeps
+// one, two measured 2464 -> 2675 us per 400^3 step)
+#ifndef CG_FAST_MINB_X20
+#define CG_FAST_MINB_X20 2
+#endif
 // rows per y-CTA and columns per x-CTA (16 threads each)
 #ifndef CG_YP
 #define CG_YP 4
@@ -52,7 +58,11 @@ template <int N>
 struct XT {
   static constexpr int TPP = PSplit<N>::TPP, THREADS = TPP * CG_XP;
   static constexpr int MINB = TPP == 16 ? CG_FAST_MINB_X : 1;
-  static constexpr int minb(int mode) { return TPP == 16 && mode != X_DIV ? CG_FAST_MINB_XG : MINB; }
+  // 320-point axis: CG_FAST_MINB_X20 CTAs per SM except for X_DIV (its
+  // parked tile needs the registers of one)
+  static constexpr int minb(int mode) {
+    return TPP == 16 ? (mode != X_DIV ? CG_FAST_MINB_XG : MINB) : (N == 320 && mode != X_DIV ? CG_FAST_MINB_X20 : MINB);
+  }
 };
 
 // One instantiation per mode keeps each kernel's code small enough for the
