@@ -43,7 +43,7 @@ def _flags(verbose_ptxas: bool = False) -> list[str]:
          f"-I{INCLUDE}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
     if verbose_ptxas:
         f.append("-Xptxas=-v")
-    for var in ("CG_FAST_MINB_Y", "CG_FAST_MINB_X", "CG_FAST_MINB_XG", "CG_FAST_MINB_X20", "CG_FAST_MINB_Z", "CG_YP", "CG_XP", "CG_ZP"):
+    for var in ("CG_FAST_MINB_Y", "CG_FAST_MINB_X", "CG_FAST_MINB_XG", "CG_FAST_MINB_X20", "CG_FAST_MINB_Z", "CG_YP", "CG_YP20", "CG_XP", "CG_ZP"):
         if os.environ.get(var):
             f.append(f"-D{var}={int(os.environ[var])}")
     return f

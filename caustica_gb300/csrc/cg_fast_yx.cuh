@@ -34,6 +34,9 @@
 #define CG_FAST_MINB_X20 2
 #endif
 // rows per y-CTA and columns per x-CTA (16 threads each)
+#ifndef CG_YP20
+#define CG_YP20 4  // rows per y-CTA on 20-thread pencils
+#endif
 #ifndef CG_YP
 #define CG_YP 4
 #endif
@@ -51,7 +54,7 @@ using cgf::static_for;
 // (20-thread pencils get the register budget that avoids spills).
 template <int N>
 struct YT {
-  static constexpr int TPP = PSplit<N>::TPP, THREADS = TPP * CG_YP;
+  static constexpr int TPP = PSplit<N>::TPP, YP = TPP == 20 ? CG_YP20 : CG_YP, THREADS = TPP * YP;
   static constexpr int MINB = TPP == 16 ? CG_FAST_MINB_Y : 4;
 };
 template <int N>
@@ -83,7 +86,7 @@ __global__ void __launch_bounds__(YT<N>::THREADS, YT<N>::MINB) kf_ypass(Dims d, 
   const int s = threadIdx.x % TPP, p = threadIdx.x / TPP;
   const Ex ex{sm + N + p * Ex::SLAB};
   const long long nrows = (long long)d.nx * d.nzh;
-  const long long row = (long long)blockIdx.x * CG_YP + p;
+  const long long row = (long long)blockIdx.x * YT<N>::YP + p;
   const bool valid = row < nrows;
   const long long off = (long long)blockIdx.y * d.nspec + row * N;
   __syncthreads();
@@ -241,7 +244,7 @@ __global__ void __launch_bounds__(XT<N>::THREADS, XT<N>::minb(MODE)) kf_xpass(Di
 // twiddles | exchange | (x: a parked spectrum tile, k_x, k_x^2)
 template <int N>
 static size_t smem_y() {
-  return sizeof(float2) * (N + CG_YP * RowEx<PSplit<N>::A, PSplit<N>::B>::SLAB);
+  return sizeof(float2) * (N + YT<N>::YP * RowEx<PSplit<N>::A, PSplit<N>::B>::SLAB);
 }
 template <int N>
 static size_t smem_x() {
@@ -252,7 +255,7 @@ static size_t smem_x() {
 template <int N>
 bool yx_launch_y(int mode, const Dims& d, const Tables& t, float2* S0, float2* S1, float2* S2, int batch,
                  cudaStream_t st) {
-  const dim3 grid((unsigned)((d.nx * (long long)d.nzh + CG_YP - 1) / CG_YP), batch);
+  const dim3 grid((unsigned)((d.nx * (long long)d.nzh + YT<N>::YP - 1) / YT<N>::YP), batch);
   const dim3 block(YT<N>::THREADS);
   switch (mode) {
     case Y_FWD: cgf::launch(kf_ypass<N, Y_FWD>, grid, block, smem_y<N>(), st, d, t, S0, S1, S2); break;
