@@ -149,6 +149,49 @@ def _uniform(flat) -> bool:
         return all(ex.map(chunk, range(0, n, step)))
 
 
+# material counts up to which label_volumes assigns labels by direct
+# comparison scans (one pass per material) instead of sorting every cell
+_SCAN_MATERIALS = 24
+
+
+def _scan_labels(bits, rows: np.ndarray):
+    """Labels by comparison: every cell gets the index of the row of
+    ``rows`` (value tuples as uint32 bit patterns) it equals bit for bit;
+    tuples absent from ``rows`` are appended in order of first occurrence.
+    Chunks run on a few host threads. None past _SCAN_MATERIALS rows."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    n = bits[0].size
+    inv = np.full(n, 255, np.uint8)
+    rows = [tuple(int(x) for x in r) for r in rows]
+    nt = max(1, min(8, os.cpu_count() or 1))
+    step = max(1 << 18, (n + 4 * nt - 1) // (4 * nt))
+
+    def assign(a, first_row):
+        b = min(n, a + step)
+        part = inv[a:b]
+        for m in range(first_row, len(rows)):
+            eq = bits[0][a:b] == np.uint32(rows[m][0])
+            for f, v in zip(bits[1:], rows[m][1:]):
+                eq &= f[a:b] == np.uint32(v)
+            part[eq & (part == 255)] = m
+
+    first_row = 0
+    while True:
+        with ThreadPoolExecutor(nt) as ex:
+            list(ex.map(lambda a: assign(a, first_row), range(0, n, step)))
+        left = np.flatnonzero(inv == 255)
+        if left.size == 0:
+            break
+        if len(rows) >= _SCAN_MATERIALS:
+            return None
+        first_row = len(rows)
+        rows.append(tuple(int(f[left[0]]) for f in bits))
+    props = np.array(rows, np.uint32).view(np.float32).reshape(len(rows), len(bits))
+    return inv, props.copy()
+
+
 def _labels_match(props: np.ndarray, inv: np.ndarray, vols) -> bool:
     """props[inv] == vols bit for bit, checked in chunks on a few host threads
     (the NumPy gathers and compares release the GIL)."""
@@ -208,10 +251,17 @@ def label_volumes(vols, id_map=None, max_labels: int = 256):
     if _uniform(flat):
         return (np.zeros(vols[0].shape, np.uint8),
                 np.array([[f[0] for f in flat]], np.float32))
-    bits = [f.view(np.uint32).astype(np.uint64) for f in flat]
-    for b in bits:
-        if len(np.unique(b[:: max(1, b.size // 4096)])) > max_labels:
+    stride = max(1, flat[0].size // 4096)
+    for f in flat:
+        if len(np.unique(f.view(np.uint32)[::stride])) > max_labels:
             return None
+    sample = np.unique(np.stack([f.view(np.uint32)[::stride] for f in flat], axis=1), axis=0)
+    if len(sample) <= _SCAN_MATERIALS:
+        got = _scan_labels([f.view(np.uint32) for f in flat], sample)
+        if got is not None:
+            inv, props = got
+            return inv.reshape(vols[0].shape), props
+    bits = [f.view(np.uint32).astype(np.uint64) for f in flat]
     keys = [(bits[i] << np.uint64(32)) | (bits[i + 1] if i + 1 < nv else np.uint64(0)) for i in range(0, nv, 2)]
     code = None
     for k in keys:

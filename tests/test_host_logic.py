@@ -162,3 +162,19 @@ def test_thermal_label_decomposition_is_exact():
     lab, props = th.thermal_labels(tm)
     for j, v in enumerate(vols):
         np.testing.assert_array_equal(props[lab, j], v)
+
+
+@pytest.mark.parametrize("n_mat", [3, 40])
+def test_label_decomposition_without_an_id_map_is_exact_for_rare_materials(n_mat):
+    """Few materials take the comparison-scan path (a material the 4096-cell
+    sample misses is appended), many take the sorting path; both are exact."""
+    rng = np.random.default_rng(n_mat)
+    shape = (40, 50, 64)
+    ids = rng.integers(0, n_mat, shape)
+    vals = np.array([[0.5 + 0.01 * i, 1000.0 + i, 3600.0 - i, 1e-4 * i] for i in range(n_mat)], np.float32)
+    vols = [vals[ids, j] for j in range(4)]
+    vols[1][7, 8, 9] = np.float32(999.25)  # one cell of a material no sample row has
+    vols[3][1, 2, 3] = np.float32(-0.0)    # differs from +0.0 only in its bit pattern
+    lab, props = eng.label_volumes(vols)
+    for j in range(4):
+        np.testing.assert_array_equal(props[lab, j].view(np.uint32), vols[j].view(np.uint32))
