@@ -75,6 +75,16 @@ def test_the_reference_planner_reads_the_entry():
         assert ref.predict_step_time(entry, p) == pytest.approx(t, rel=1e-6)
     mid = ref.predict_step_time(entry, 200 ** 3)
     assert entry["samples"][1][1] < mid < entry["samples"][2][1]
+    # the same fit and residual as the reference's on the same samples
+    rng = np.random.default_rng(11)
+    for _ in range(5):
+        samples = [(int(p), float(t)) for p, t in zip(sorted(rng.integers(10 ** 6, 10 ** 9, 3)),
+                                                      sorted(rng.uniform(1e-4, 1e-1, 3)))]
+        a, b = cal.fit_time_model(samples)
+        ra, rb = ref.fit_time_model(samples)
+        assert a == pytest.approx(ra, rel=1e-9, abs=1e-30) and b == pytest.approx(rb, rel=1e-9, abs=1e-30)
+        assert cal.max_rel_residual(samples, a, b) == pytest.approx(ref.fit_max_rel_residual(samples, ra, rb),
+                                                                     rel=1e-9)
 
 
 @pytest.mark.gpu
