@@ -3,10 +3,11 @@
 // cg_fast_yx_*.cu units (a few lengths each, so they compile in parallel)
 // and dispatched by cg_fast_yx.cu.
 //
-// y-pass: rows (x, kz) of length ny, 16 rows per CTA; thread (p, s) =
-// (threadIdx / 16, threadIdx % 16) owns row p. x-pass: 16 consecutive
-// (kz, y) columns per CTA; thread (c, s) = (threadIdx % 16, threadIdx / 16)
-// owns column c. Pencil data moves global -> registers -> one exchange per
+// y-pass: rows (x, kz) of length ny, YP rows per CTA; thread (p, s) =
+// (threadIdx / TPP, threadIdx % TPP) owns row p (TPP = threads per pencil:
+// 16, or 20 / 32 for the 320/400 and 512/640 splits). x-pass: CG_XP
+// consecutive (kz, y) columns per CTA; thread (c, s) = (threadIdx % CG_XP,
+// threadIdx / CG_XP) owns column c. Pencil data moves global -> registers -> one exchange per
 // transform -> registers -> global (cg_fast.cuh).
 #pragma once
 

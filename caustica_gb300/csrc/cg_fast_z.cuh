@@ -4,8 +4,9 @@
 // cg_fast_z.cu.
 //
 // Tile = (batch member, x, 32 consecutive y). Real rows y0+2p and y0+2p+1
-// form complex pencil p (p = threadIdx / 16); s = threadIdx % 16 runs along
-// the pencil. The inverse (complex-to-real) transform is an (A, B) fft2, the
+// form complex pencil p (p = threadIdx / TPP, TPP = threads per pencil: 16,
+// or 20 / 32 for the 320/400 and 512/640 splits); s = threadIdx % TPP runs
+// along the pencil. The inverse (complex-to-real) transform is an (A, B) fft2, the
 // forward one a (B, A) fft2, so the values produced by the inverse arrive in
 // exactly the registers the forward transform reads; the pointwise update
 // runs in between, on cells (x, y, s + A b) with coalesced row accesses.
