@@ -175,7 +175,8 @@ def slot_symbols(padded3) -> list[str]:
     zp = "kfp" if ny % 32 == 0 else "kf"
     zfast = nz in (FAST_XYZ_SIZES if zp == "kfp" else FAST_SIZES)
     zu = f"{zp}_zpass_u<{nz}>" if zfast else "k_zpass_u"
-    zpp = (f"{zp}_zpass_p<{nz}>" if zp == "kfp" else f"kf_zpass_p<{nz},1>") if zfast else "k_zpass_p"
+    # the timed steps do not record: the persistent p-pass runs its record-free instantiation
+    zpp = (f"{zp}_zpass_p<{nz},false>" if zp == "kfp" else f"kf_zpass_p<{nz},1>") if zfast else "k_zpass_p"
     return [y.format("Y_FWD"), x.format("X_GRAD"), y.format("Y_INV_GRAD"), zu, y.format("Y_FWD_DIV"),
             x.format("X_DIV"), y.format("Y_INV"), zpp]
 
