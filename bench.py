@@ -164,15 +164,17 @@ def _traffic_from_profiles(kernel: str):
 SLOTS = ["k_ypass:fwd", "k_xpass:grad", "k_ypass:inv_grad", "k_zpass_u", "k_ypass:fwd_div", "k_xpass:div",
          "k_ypass:inv", "k_zpass_p"]
 FAST_SIZES = {8, 16, 24, 32, 48, 64, 96, 128, 160, 192, 256}  # every size-specialised kernel family
-FAST_XYZ_SIZES = FAST_SIZES | {320, 512}  # x/y passes and the persistent z-passes only
+FAST_XYZ_SIZES = FAST_SIZES | {320, 400, 512, 640}  # x/y passes and the persistent z-passes only
 
 
-def slot_symbols(padded3) -> list[str]:
-    """The kernel each step slot launches on this grid (size-specialised where the axis allows)."""
+def slot_symbols(padded3, persistent_z: bool = True) -> list[str]:
+    """The kernel each step slot launches on this grid (size-specialised where the axis allows);
+    ``persistent_z`` is the autotuner's z-pass choice (lengths without a per-tile kernel are always
+    persistent when ny is even)."""
     nx, ny, nz = padded3
     y = f"kf_ypass<{ny},{{}}>" if ny in FAST_XYZ_SIZES else "k_ypass"
     x = f"kf_xpass<{nx},{{}}>" if nx in FAST_XYZ_SIZES else "k_xpass"
-    zp = "kfp" if ny % 32 == 0 else "kf"
+    zp = "kfp" if ny % 2 == 0 and (persistent_z or nz not in FAST_SIZES) else "kf"
     zfast = nz in (FAST_XYZ_SIZES if zp == "kfp" else FAST_SIZES)
     zu = f"{zp}_zpass_u<{nz}>" if zfast else "k_zpass_u"
     # the timed steps do not record: the persistent p-pass runs its record-free instantiation
@@ -305,6 +307,7 @@ def run_gb300(args, dist, rank, ws, local):
     dom = int(np.argmax(per_launch_ms))
     achieved = bytes_slot[dom] / (per_launch_ms[dom] * 1e-3) / 1e9
     kernel_name = SLOTS[dom]
+    symbols = slot_symbols(plan.padded3, bool((tuning or {}).get("persistent_z", True)))
     traffic = _traffic_from_profiles(kernel_name)
     step_b = step_algorithmic_bytes(info_labels, True)
     step_achieved = step_b * value / ws / 1e9
@@ -320,7 +323,7 @@ def run_gb300(args, dist, rank, ws, local):
                                                                            "direct launches"),
                        "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush",
                        "tuning": tuning},
-            "roofline": {"bound": "hbm", "kernel": kernel_name, "kernel_symbol": slot_symbols(plan.padded3)[dom],
+            "roofline": {"bound": "hbm", "kernel": kernel_name, "kernel_symbol": symbols[dom],
                          "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_launch": bytes_slot[dom],
                          "ms_per_launch": float(per_launch_ms[dom]), "traffic": traffic},
