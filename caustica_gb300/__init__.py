@@ -18,6 +18,7 @@ from .contract import (
     SolverDivergedError,
     SolverResult,
 )
+from .checkpoint import CheckpointMismatch, CheckpointSpec, RunInterrupted
 from .metrics import FieldFrame, device_focus_metrics, focus_metrics
 from .sensors import HeatingSource
 from .solvers import LinearKSpaceGB300, WesterveltKSpaceGB300, get
@@ -26,6 +27,7 @@ from .thermal import PennesSolverGB300, ThermalMedium, ThermalResult
 __all__ = [
     "CWRunSpec", "CWSource", "Grid", "Medium", "PMLSpec", "SolverCapabilityError", "SolverDivergedError",
     "SolverResult", "LinearKSpaceGB300", "WesterveltKSpaceGB300", "get", "PennesSolverGB300", "ThermalMedium",
-    "ThermalResult", "FieldFrame", "focus_metrics", "device_focus_metrics", "HeatingSource",
+    "ThermalResult", "FieldFrame", "focus_metrics", "device_focus_metrics", "HeatingSource", "CheckpointSpec",
+    "CheckpointMismatch", "RunInterrupted",
 ]
 __version__ = "0.1.0"

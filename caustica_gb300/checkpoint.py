@@ -83,6 +83,7 @@ def fingerprint(plan: Plan, grid, medium, source) -> dict[str, Any]:
         "dx": plan.dx, "pml_vox": int(plan.pml3[2]), "pml_edge": plan.pml_edge, "spp": plan.spp, "f0": plan.f0,
         "amplitude": plan.amplitude, "ramp_periods": plan.ramp_periods, "harmonics": list(plan.harmonics),
         "nonlinear": plan.nonlinear_active, "record_region": [[s.start, s.stop] for s in plan.rec],
+        "reference_point": plan.meta.get("reference_point"),
         "spec": {k: v for k, v in dump.items()},
         "source_sha1": arrays_sha1(source.indices, source.phases),
         "medium_sha1": arrays_sha1(medium.c, medium.rho, medium.alpha, medium.beta),
@@ -149,13 +150,20 @@ def _restore(dev: DeviceSolver, plan: Plan, fields: dict, n: int) -> None:
 
 
 def run_with_checkpoint(plan: Plan, checkpoint, *, progress=None, result_cls, grid, medium, source):
-    """Period-by-period solve with checkpoint cadence, resume and graceful stop."""
+    """Period-by-period solve with checkpoint cadence, resume and graceful stop.
+
+    The settle loop, the period-boundary order (progress, then the cadence
+    write, then the stop poll), the t_end floor and the pre-record snapshot
+    follow engine.py:436-451, 484-534. A checkpoint that belongs to another
+    run is refused before any device memory is taken.
+    """
     t0 = time.monotonic()
     spec = plan.spec
     fp = fingerprint(plan, grid, medium, source)
     every = int(getattr(checkpoint, "every_periods", 8))
     stop_when = getattr(checkpoint, "stop_when", None)
     path = Path(checkpoint.path)
+    state = load(path, fp)
     with DeviceSolver(plan) as dev:
         n = 0
         prev_peak = None
@@ -164,7 +172,6 @@ def run_with_checkpoint(plan: Plan, checkpoint, *, progress=None, result_cls, gr
         history: list = []
         periods_done = 0
         stage = "settle"
-        state = load(path, fp)
         if state is not None:
             _restore(dev, plan, state["fields"], state["n"])
             n, periods_done = state["n"], state["periods_done"]
@@ -174,6 +181,15 @@ def run_with_checkpoint(plan: Plan, checkpoint, *, progress=None, result_cls, gr
         def save(stage_now):
             write(path, stage=stage_now, n=n, periods_done=periods_done, prev_peak=prev_peak, converged=converged,
                   converged_period=converged_period, history=history, fields=_fields(dev, plan), fp=fp)
+
+        def boundary(peak, rel):
+            if progress is not None:
+                _emit(progress, plan, dev, "settle", periods_done, peak, rel, t0)
+            stop = stop_when is not None and stop_when()
+            if stop or periods_done % every == 0:
+                save("settle")
+            if stop:
+                raise RunInterrupted(path, "settle", periods_done, n)
 
         period_idx = periods_done
         while stage == "settle" and not converged and period_idx < plan.eff_max:
@@ -191,21 +207,18 @@ def run_with_checkpoint(plan: Plan, checkpoint, *, progress=None, result_cls, gr
                 converged = True
             if not converged:
                 prev_peak = peak
-            if progress is not None:
-                _emit(progress, plan, dev, "settle", period_idx, peak, rel, t0)
-            stop = stop_when is not None and stop_when()
-            if stop or periods_done % every == 0:
-                save("settle")
-            if stop:
-                raise RunInterrupted(path, "settle", periods_done, n)
+            boundary(peak, rel)
         if spec.t_end_min_us is not None and stage == "settle":
             need = int(np.ceil(spec.t_end_min_us * 1e-6 / plan.period)) - spec.n_record_periods
             while periods_done < need:
                 dev.run_periods(1)
                 n += plan.spp
                 periods_done += 1
+                boundary(None, None)
         if stage == "settle":
             stage = "record"
+            if progress is not None:
+                _emit(progress, plan, dev, "record", periods_done, None, None, t0)
             save("record")
             if stop_when is not None and stop_when():
                 raise RunInterrupted(path, "record", periods_done, n)

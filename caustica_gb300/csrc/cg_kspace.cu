@@ -1543,7 +1543,10 @@ static void* g_noalloc_ptr[128];  // per-device address of g_noalloc_twiddles
 
 // Once per device, with that device current: resolve the array's device
 // address (the host-side symbol is only a stand-in) and lift the kernels'
-// dynamic shared-memory limit. Neither allocates.
+// dynamic shared-memory limit. Neither allocates. Both results are kept for
+// the life of the process, so destroying a device's primary context while
+// the library is loaded (cudaDeviceReset) is not supported: the next call
+// would launch against the old context's address.
 static int noalloc_setup(int dev, float2** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
@@ -1575,9 +1578,14 @@ extern "C" int cg_fft3d_forward_noalloc(int nx, int ny, int nz, int batch, const
     cg_set_error("FFT shape %dx%dx%d: every axis must be 2/3/5-smooth", nx, ny, nz);
     return CG_ERR_INVALID;
   }
+  // this entry point always launches the runtime-plan passes below, so all
+  // three of their tiles must fit (on a 227 KB device: ny <= 540, nx <= 576,
+  // nz <= 810), whether or not a size-specialised pass exists for an axis;
+  // the check runs before anything is queued, so a refused call writes nothing
   const size_t sy = smem_ypass(ny), sx = smem_xpass(nx), sz = smem_zpass(nz), lim = smem_limit();
-  CG_REQUIRE((fast_xy_has(ny) || sy <= lim) && (fast_xy_has(nx) || sx <= lim) && sz <= lim,
-             "FFT shape %dx%dx%d needs more shared memory per tile than the device offers", nx, ny, nz);
+  CG_REQUIRE(sy <= lim && sx <= lim && sz <= lim,
+             "FFT shape %dx%dx%d needs more shared memory per tile than the device offers "
+             "(y tile %zu, x tile %zu, z tile %zu bytes; limit %zu)", nx, ny, nz, sy, sx, sz, lim);
   int dev = 0;
   CG_CUDA_TRY(cudaGetDevice(&dev));
   CG_REQUIRE(dev >= 0 && dev < 128, "device ordinal %d out of range", dev);

@@ -443,6 +443,7 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
         ramp_periods=float(source.ramp_periods), labels=labels, label_table=table, label_props=props,
         dense=dense,
         label=getattr(source, "label", ""),
+        meta={"reference_point": None if reference_point is None else [int(r) for r in reference_point]},
     )
 
 

@@ -22,6 +22,7 @@ and without backend, checkpoint and progress options.
 
 from __future__ import annotations
 
+import dataclasses
 from typing import Any
 
 from caustica.io.checkpoint import CheckpointMismatch as _CkMismatch
@@ -109,9 +110,11 @@ def install_compat() -> None:
         original = planner.estimate
 
         def estimate(*args, solver: str = "westervelt", **kwargs):
-            if solver.endswith("_gb300"):
-                solver = solver[: -len("_gb300")]
-            return original(*args, solver=solver, **kwargs)
+            if not solver.endswith("_gb300"):
+                return original(*args, solver=solver, **kwargs)
+            est = original(*args, solver=solver[: -len("_gb300")], **kwargs)
+            # the verdict names the solver that will run
+            return dataclasses.replace(est, solver=solver) if dataclasses.is_dataclass(est) else est
 
         estimate._gb300_wrapped = True  # type: ignore[attr-defined]
         planner.estimate = estimate

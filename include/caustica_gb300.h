@@ -145,12 +145,16 @@ int cg_fft3d_inverse(cg_fft3d* f, const float* in_spec, float* out);
  * work is queued on `stream` (a cudaStream_t, NULL = legacy default) and
  * the call returns without synchronising. The only scratch, three per-axis
  * twiddle tables, lives in a fixed 48 KB device array that every GPU which
- * loads the library keeps until the process exits; every axis must be
- * <= 2048 (larger shapes are refused with CG_ERR_INVALID). The first call on
- * a device resolves that array's address there, so make it before any
- * stream capture. Calls share the array and rewrite it in full: calls whose
- * work overlaps on the GPU (different streams, no ordering) race. No
- * cudaMalloc, cudaFree or allocating library call is made. */
+ * loads the library keeps until the process exits; that array bounds every
+ * axis at 2048. The transform's shared-memory tiles bound them further: on a
+ * device with 227 KB per block (GB300) ny <= 540, nx <= 576 and nz <= 810.
+ * Larger shapes are refused with CG_ERR_INVALID before anything is queued.
+ * The first call on a device resolves that array's address there, so make
+ * it before any stream capture; the address is kept for the process, so
+ * cudaDeviceReset while the library is loaded is not supported. Calls share
+ * the array and rewrite it in full: calls whose work overlaps on the GPU
+ * (different streams, no ordering) race. No cudaMalloc, cudaFree or
+ * allocating library call is made. */
 int cg_fft3d_forward_noalloc(int nx, int ny, int nz, int batch, const float* in_dev, float* out_dev,
                              void* stream);
 

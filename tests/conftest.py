@@ -3,6 +3,7 @@
 from __future__ import annotations
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -13,6 +14,20 @@ ROOT = Path(__file__).resolve().parent.parent
 GOLDEN = Path(__file__).resolve().parent / "golden"
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
+
+
+def reference_src() -> Path | None:
+    """Source tree of the reference package (the directory holding ``caustica/``).
+
+    Taken from ``CAUSTICA_REFERENCE_SRC``, else a ``reference/src`` checkout
+    beside this repository; None when neither exists (tests that need the
+    reference then skip; the GPU tests never do).
+    """
+    cands = [os.environ.get("CAUSTICA_REFERENCE_SRC"), ROOT.parent / "reference" / "src"]
+    for cand in cands:
+        if cand and (Path(cand) / "caustica" / "__init__.py").exists():
+            return Path(cand)
+    return None
 
 
 def pytest_configure(config):

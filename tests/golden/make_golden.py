@@ -270,4 +270,9 @@ def main(src_path: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    import os
+
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CAUSTICA_REFERENCE_SRC")
+    if not src:
+        sys.exit("usage: make_golden.py /path/to/caustica/src  (or set CAUSTICA_REFERENCE_SRC)")
+    main(src)

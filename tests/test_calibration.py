@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from caustica_gb300 import calibration as cal
+from conftest import reference_src
 
 # the fields of the reference's calibration entry (planner/calibration.py:536-570)
 REFERENCE_ENTRY_KEYS = {"a", "b", "fit_mode", "global_fit_mode", "fit_max_rel_residual", "interp_loo_rel_err",
@@ -62,9 +63,9 @@ def test_entry_has_the_reference_schema_and_merges_into_the_file(tmp_path):
 
 
 def test_the_reference_planner_reads_the_entry():
-    src = Path("/root/reference/src")
-    if not (src / "caustica" / "planner" / "calibration.py").exists():
-        pytest.skip("reference sources not present")
+    src = reference_src()
+    if src is None or not (src / "caustica" / "planner" / "calibration.py").exists():
+        pytest.skip("reference sources not present (set CAUSTICA_REFERENCE_SRC)")
     sys.path.insert(0, str(src))
     try:
         ref = pytest.importorskip("caustica.planner.calibration")
