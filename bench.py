@@ -202,8 +202,11 @@ def step_algorithmic_bytes(labels: bool, nonlinear: bool) -> int:
     return 84 if nonlinear else 80
 
 
-def cpu_sample(job, target_s: float = 12.0, workers: int | None = None):
-    """Time the reference's float32 NumPy step (oracle restatement) on this host."""
+def cpu_sample(job, target_s: float = 12.0, workers: int | None = None, max_steps: int = 200, min_steps: int = 1,
+               time_cap: float | None = None):
+    """Time the reference's float32 NumPy step (oracle restatement) on this host:
+    at least ``min_steps`` and ``target_s`` seconds, at most ``max_steps``
+    steps, and never past ``time_cap`` seconds."""
     from caustica_gb300 import engine as eng
     from oracle import kspace as ok
 
@@ -229,7 +232,9 @@ def cpu_sample(job, target_s: float = 12.0, workers: int | None = None):
                            sponge=spg, deriv=der, padded=shape)
             n += 1
             el = time.perf_counter() - t0
-            if el >= target_s or n >= 200:
+            if n >= max_steps or (el >= target_s and n >= min_steps):
+                break
+            if time_cap is not None and el >= time_cap:
                 break
     cells = int(np.prod(shape))
     return {"value": cells * n / el, "unit": UNIT, "cores": workers, "kind": "port",
@@ -237,21 +242,40 @@ def cpu_sample(job, target_s: float = 12.0, workers: int | None = None):
                       f"({el:.1f} s, scipy.fft workers={workers})", "steps": n, "seconds": el}
 
 
+def workload_config(job) -> dict:
+    """The ``config`` keys both arms print for the benchmark workload."""
+    from caustica_gb300 import engine as eng
+
+    grid, med, src, spec = job["grid"], job["medium"], job["source"], job["spec"]
+    spp, _ = eng.cw_discretization(grid.dx, float(med.c.max()), src.f0, spec, job["harmonics"])
+    n_mat = len(np.unique(med.id_map)) if getattr(med, "id_map", None) is not None else None
+    return {"workload": job["name"], "grid": list(grid.shape), "cells": int(np.prod(grid.shape)),
+            "harmonics": list(job["harmonics"]),
+            "medium": f"{n_mat} labels (uint8 map)" if n_mat is not None else "dense float32 maps",
+            "source_voxels": int(src.indices.shape[0]), "spp": spp,
+            "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush"}
+
+
 def run_reference(args, dist, rank):
+    """The reference's CPU step (float32 NumPy/SciPy, all host cores): W
+    untimed warm-up steps, then K timed steps, both cut short when the
+    sample would outlast its time budget (the line reports the steps run)."""
     from caustica_gb300 import workloads as wl
 
     if rank != 0:
         return
     job = wl.config2()
     budget = float(os.environ.get("CG_REFERENCE_SECONDS", "45"))
-    # warm-up: one step (plans and page faults), then a bounded sample
-    cpu_sample(job, target_s=0.0)
-    s = cpu_sample(job, target_s=budget)
+    warm = cpu_sample(job, target_s=0.0, max_steps=max(1, int(args.warmup)), min_steps=max(1, int(args.warmup)),
+                      time_cap=budget / 4)
+    s = cpu_sample(job, target_s=budget, max_steps=int(args.steps), min_steps=int(args.steps), time_cap=budget)
+    cfg = workload_config(job)
+    cfg["timing"] = "wall clock of each NumPy/SciPy step on the host cores"
     line = {"impl": "reference", "metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": s["steps"], "warmup": 1, "ms_per_step": 1e3 * s["seconds"] / s["steps"],
+            "steps": s["steps"], "warmup": warm["steps"], "steps_requested": int(args.steps),
+            "warmup_requested": int(args.warmup), "ms_per_step": 1e3 * s["seconds"] / s["steps"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": job["name"], "grid": list(job["grid"].shape), "harmonics": list(job["harmonics"]),
-                       "l2": "inputs larger than L2"},
+            "config": cfg,
             "cpu_baseline": {k: s[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": s["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line, default=_jsonable), flush=True)
@@ -316,17 +340,17 @@ def run_gb300(args, dist, rank, ws, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": t_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": job["name"], "grid": list(plan.padded3), "cells": ncell,
-                       "harmonics": list(plan.harmonics), "medium": f"{len(plan.label_table)} labels (uint8 map)",
-                       "source_voxels": int(plan.src_xyz.shape[0]), "spp": plan.spp,
+            "config": {**workload_config(job),
                        "timing": "CUDA events on the solver stream, " + ("CUDA graph per period" if graph else
                                                                            "direct launches"),
-                       "l2": "inputs larger than L2 (p,u 151 MB + spectra 114 MB > 129 MB L2); no flush",
                        "tuning": tuning},
             "roofline": {"bound": "hbm", "kernel": kernel_name, "kernel_symbol": symbols[dom],
                          "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_launch": bytes_slot[dom],
-                         "ms_per_launch": float(per_launch_ms[dom]), "traffic": traffic},
+                         "ms_per_launch": float(per_launch_ms[dom]), "traffic": traffic,
+                         "traffic_source": None if traffic is None else
+                         "profiles/traffic_per_launch.txt: ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                         "this kernel in one config-2 step (committed capture, not measured in this run)"},
             "step_roofline": {"bytes_per_cell_step": step_b, "achieved": step_achieved, "peak": hbm,
                               "frac": step_achieved / hbm, "unit": "GB/s",
                               "note": "algorithmic bytes of the fully fused step with label-indexed maps"},
@@ -349,7 +373,10 @@ def run_gb300(args, dist, rank, ws, local):
                + 16 * plan.max_periods * plan.spp)
         d2h = sum(v.nbytes for v in res.phasors.values()) + res.p_max.nbytes
         e2e_value = ws * ncell * res.steps_total / el
-        line["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        # the metric's step is one time step: the solve's copies spread over its steps
+        line["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / res.steps_total,
+                       "d2h_bytes_per_step": d2h / res.steps_total, "h2d_bytes_per_solve": h2d,
+                       "d2h_bytes_per_solve": d2h,
                        "step": f"one full solve ({res.steps_total} time steps, {res.steps_total // plan.spp} periods) "
                                f"through WesterveltKSpaceGB300.run() from host numpy",
                        "seconds": el, "solves_per_s": ws / el}
@@ -362,6 +389,9 @@ def run_gb300(args, dist, rank, ws, local):
     if rank == 0 and ws == 1 and not args.skip_cpu:
         cb = cpu_sample(job, target_s=float(os.environ.get("CG_CPU_SECONDS", "12")))
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # the same step with one FFT worker (the reference's set_cpu_fft_workers(1), core/backend.py:84-91)
+        c1 = cpu_sample(job, target_s=float(os.environ.get("CG_CPU1_SECONDS", "8")), workers=1, max_steps=40)
+        line["cpu_baseline_1worker"] = {k: c1[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line["clocks"] = clk.summary()
     if rank == 0:
         print(json.dumps(line, default=_jsonable), flush=True)
