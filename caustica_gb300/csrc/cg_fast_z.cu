@@ -1,6 +1,7 @@
 // Dispatch of the size-specialised z-passes to the per-length launchers
 // (cg_fast_z.cuh, instantiated by the cg_fast_z_*.cu units).
 #include <cuda_runtime.h>
+#include <string.h>
 
 #include "cg_kspace.cuh"
 
@@ -10,6 +11,9 @@ void zp_run_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, floa
 template <int N>
 void zp_run_p(const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src, const RecordDev& rec,
               const long long* ctl, int n_local, int record, float* p, float2* S0, int batch, cudaStream_t st);
+template <int N>
+void zp_run_fwd(const Dims& d, const Tables& t, const MediumDev& m, float* p, float2* S0, int batch,
+                cudaStream_t st);
 template <int N>
 int zp_prepare();
 template <int N>
@@ -72,6 +76,29 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
     default:
       return false;
   }
+}
+
+bool fast_zpass_fwd_step(const Dims& d, const Tables& t, const MediumDev& m, float* p, float2* S0, int batch,
+                         cudaStream_t st, bool persistent) {
+  // the kernel family the step's p-pass runs on this grid (fast_zpass_p, mode 1)
+  if ((persistent || !fast_has(d.nz)) && d.ny % 2 == 0) {
+    switch (d.nz) {
+#define CASE(n)                                      \
+  case n:                                            \
+    zp_run_fwd<n>(d, t, m, p, S0, batch, st);        \
+    return true;
+      CG_FAST_ZSIZES(CASE)
+#undef CASE
+      default:
+        return false;
+    }
+  }
+  SourceDev src;
+  memset(&src, 0, sizeof(src));
+  RecordDev rec;
+  memset(&rec, 0, sizeof(rec));
+  rec.spp = 1;
+  return fast_zpass_p(0, d, t, m, src, rec, nullptr, 0, 0, p, S0, batch, st, false);
 }
 
 int fast_prepare_z() {

@@ -14,6 +14,8 @@
 // spectral layout has y fastest, the real layout z fastest).
 #pragma once
 
+#include <string.h>
+
 #include "cg_fast.cuh"
 #include "cg_kspace.cuh"
 
@@ -637,7 +639,10 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
 
 // REC: the step records into the phase bins (an instantiation without the
 // record path keeps the non-recording steps' instruction stream short).
-template <int N, bool REC>
+// FWD: only the closing forward transform, of the pressure as it is -- the
+// spectrum a step leaves behind, rebuilt from a restored pressure field by
+// the very code the step runs, so a restored run continues bit for bit.
+template <int N, bool REC, bool FWD = false>
 __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpass_p(Dims d, Tables t, MediumDev m,
                                                                        SourceDev src, RecordDev rec,
                                                                        const long long* ctl, int n_local, int record,
@@ -670,6 +675,29 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     if (lab) z_prefetch_labels<N>(lab0 + j * CG_ZROWS * N, m.labels, d, x, y0);
     cgf::cp_async_commit();
   };
+  if constexpr (FWD) {
+    int jf = 0;
+    for (long long tile = t0; tile < t1; ++tile, jf ^= 1) {
+      const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
+      const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
+      const int ya = y0 + 2 * p;
+      const bool va = ya < d.ny;  // ny even: row ya + 1 too
+      const float* pb = p_all + b_idx * d.ncell;
+      const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
+      float2 w[B];
+      if (s < A) static_for<0, B>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        const int n = s + A * b;
+        w[b] = make_float2(va ? __ldg(pb + rowa + n) : 0.f, va ? __ldg(pb + rowb + n) : 0.f);
+      });
+      float2* bufj = sm + Z::OFF_BUF + (size_t)jf * Z::BUF;
+      const RowEx<B, A> exf{bufj + p * Z::EX};
+      float2 X[A];
+      fft2<B, A, false>(w, X, s, sm + N, exf);
+      z_split_store<N>(bufj, X, S0 + b_idx * d.nspec, d, x, y0, p, s, nullptr);
+    }
+    return;
+  }
   prefetch(t0, 0);
   const long long n_step = ctl[0] + n_local;
   const int m_bin = (int)(n_step % rec.spp);
@@ -836,9 +864,25 @@ void zp_run_p(const Dims& d, const Tables& t, const MediumDev& m, const SourceDe
 }
 
 template <int N>
+void zp_run_fwd(const Dims& d, const Tables& t, const MediumDev& m, float* p, float2* S0, int batch,
+                cudaStream_t st) {
+  int g = 0, per = 0;
+  cgf::persistent_grid((long long)d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS) * batch, ZPShape<N>::MINB, &g, &per);
+  SourceDev src;
+  memset(&src, 0, sizeof(src));
+  RecordDev rec;
+  memset(&rec, 0, sizeof(rec));
+  rec.spp = 1;
+  cgf::launch(kfp_zpass_p<N, false, true>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, src,
+              rec, (const long long*)nullptr, 0, 0, p, S0, batch, per);
+}
+
+template <int N>
 int zp_prepare() {
   const int sm = (int)ZPShape<N>::smem;
   return (cudaFuncSetAttribute(kfp_zpass_u<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
+          cudaFuncSetAttribute(kfp_zpass_p<N, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) !=
+              cudaSuccess ||
           cudaFuncSetAttribute(kfp_zpass_p<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
           cudaFuncSetAttribute(kfp_zpass_p<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
              ? -1
@@ -884,6 +928,7 @@ int zt_prepare() {
                             cudaStream_t);                                                                         \
   template void zp_run_p<n>(const Dims&, const Tables&, const MediumDev&, const SourceDev&, const RecordDev&,     \
                             const long long*, int, int, float*, float2*, int, cudaStream_t);                      \
+  template void zp_run_fwd<n>(const Dims&, const Tables&, const MediumDev&, float*, float2*, int, cudaStream_t); \
   template int zp_prepare<n>();
 #define CG_ZT_INSTANTIATE(n)                                                                                       \
   template void zt_run_u<n>(const Dims&, const Tables&, const MediumDev&, float*, float2*, float2*, float2*, int,  \

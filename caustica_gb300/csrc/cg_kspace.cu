@@ -1004,9 +1004,121 @@ extern "C" int cg_solver_reset(cg_solver* s) {
   return CG_OK;
 }
 
-// One step = 8 launches. With `ev` (9 events) an event is recorded before
-// each launch and after the last, for per-kernel timing.
-static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = nullptr) {
+// Per-launch event log of one step: an event before each launch and one
+// after the last, each launch tagged with its slot of the step (0 y fwd,
+// 1 x grad, 2 y inv grad, 3 z u, 4 y fwd div, 5 x div, 6 y inv, 7 z p).
+struct EvLog {
+  static constexpr int kMax = 2 + 6 * CG_MAX_SLABS + 1;
+  cudaEvent_t ev[kMax];
+  int slot[kMax];
+  int n = 0;
+  void mark(int sl, cudaStream_t st) {
+    slot[n] = sl;
+    cudaEventRecord(ev[n++], st);
+  }
+};
+
+// The x-planes [x0, x0 + n) of the solver's grid as a grid of their own for
+// the plane-local (y and z) passes: offset field, spectrum, medium, source
+// and sponge pointers, record and convergence boxes shifted by x0. Member
+// strides (ncell, nspec) stay those of the whole grid.
+struct Slab {
+  Dims d;
+  Tables t;
+  MediumDev m;
+  SourceDev src;
+  RecordDev rec;
+  float *p, *u;
+  float2 *S0, *S1, *S2;
+};
+
+static Slab make_slab(const cg_solver* s, int x0, int n) {
+  Slab sl;
+  const long long cell0 = (long long)x0 * s->d.ny * s->d.nz;
+  const long long spec0 = (long long)x0 * s->d.nzh * s->d.ny;
+  sl.d = s->d;
+  sl.d.nx = n;
+  sl.t = make_tables(s);
+  sl.t.sx = s->sx + x0;
+  sl.m = make_medium(s);
+  if (sl.m.labels) sl.m.labels += cell0;
+  if (sl.m.dtr) {
+    sl.m.dtr += cell0;
+    sl.m.rc2 += cell0;
+    sl.m.ab += cell0;
+    if (sl.m.b2) sl.m.b2 += cell0;
+  }
+  sl.src = make_source(s);
+  if (sl.src.row_ptr) sl.src.row_ptr += (long long)x0 * s->d.ny;
+  sl.rec = make_record(s);
+  sl.rec.lo[0] -= x0;
+  sl.rec.hi[0] -= x0;
+  sl.rec.clo[0] -= x0;
+  sl.rec.chi[0] -= x0;
+  sl.p = s->p + cell0;
+  sl.u = s->u + cell0;
+  sl.S0 = s->S0 + spec0;
+  sl.S1 = s->S1 + spec0;
+  sl.S2 = s->S2 + spec0;
+  return sl;
+}
+
+// Slab mode needs the size-specialised y-pass and the persistent z-passes.
+static bool slabs_supported(const Dims& d) {
+  return d.nx >= 2 && d.ny % 2 == 0 && fast_xy_has(d.ny) && fast_xy_has(d.nx) && fast_xy_has(d.nz);
+}
+
+// One step in slab mode: x grad, then per slab [y inv grad, z u, y fwd div],
+// x div, then per slab [y inv, z p, y fwd]. The pressure spectrum leaves the
+// step y- and z-transformed, which is what the next step's x grad reads.
+static int launch_step_slabs(cg_solver* s, int n_local, int record, EvLog* log) {
+  const Dims d = s->d;
+  const Tables t = make_tables(s);
+  const int B = s->B;
+  const int K = s->slabs;
+  cudaStream_t st = s->stream;
+  bool ok = true;
+  auto mark = [&](int sl) {
+    if (log) log->mark(sl, st);
+  };
+  auto x0_of = [&](int k) { return (int)((long long)d.nx * k / K); };
+  mark(1);
+  ok = ok && fast_xpass(X_GRAD, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st);
+  for (int k = 0; k < K && ok; ++k) {
+    const int x0 = x0_of(k), n = x0_of(k + 1) - x0;
+    const Slab sl = make_slab(s, x0, n);
+    mark(2);
+    ok = ok && fast_ypass(Y_INV_GRAD, sl.d, sl.t, sl.S0, sl.S1, sl.S2, B, st);
+    mark(3);
+    ok = ok && fast_zpass_u(sl.d, sl.t, sl.m, sl.u, sl.S0, sl.S1, sl.S2, B, st, true);
+    mark(4);
+    ok = ok && fast_ypass(Y_FWD_DIV, sl.d, sl.t, sl.S0, sl.S1, sl.S2, B, st);
+  }
+  mark(5);
+  ok = ok && fast_xpass(X_DIV, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st);
+  for (int k = 0; k < K && ok; ++k) {
+    const int x0 = x0_of(k), n = x0_of(k + 1) - x0;
+    const Slab sl = make_slab(s, x0, n);
+    mark(6);
+    ok = ok && fast_ypass(Y_INV, sl.d, sl.t, sl.S0, sl.S1, sl.S2, B, st);
+    mark(7);
+    ok = ok && fast_zpass_p(1, sl.d, sl.t, sl.m, sl.src, sl.rec, s->ctl, n_local, record, sl.p, sl.S0, B, st, true);
+    mark(0);
+    ok = ok && fast_ypass(Y_FWD, sl.d, sl.t, sl.S0, sl.S1, sl.S2, B, st);
+  }
+  if (log) cudaEventRecord(log->ev[log->n], st);
+  if (!ok) {
+    cg_set_error("slab step: a size-specialised pass is missing for grid %dx%dx%d", d.nx, d.ny, d.nz);
+    return CG_ERR_INVALID;
+  }
+  return CG_OK;
+}
+
+// One step = 8 launches (or 2 + 6 per slab in slab mode). With `log` an
+// event is recorded before each launch and after the last, for per-kernel
+// timing.
+static int launch_step(cg_solver* s, int n_local, int record, EvLog* log = nullptr) {
+  if (s->slabs > 1) return launch_step_slabs(s, n_local, record, log);
   const Dims d = s->d;
   const Tables t = make_tables(s);
   const MediumDev m = make_medium(s);
@@ -1015,55 +1127,68 @@ static int launch_step(cg_solver* s, int n_local, int record, cudaEvent_t* ev = 
   const dim3 gy((unsigned)((d.nx * (long long)d.nzh + CG_TILE - 1) / CG_TILE), B);
   const dim3 gx((unsigned)(((long long)d.nzh * d.ny + CG_TILE - 1) / CG_TILE), B);
   const dim3 gz((unsigned)(d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS)), B);
-#define EV(i) \
-  if (ev) cudaEventRecord(ev[i], st)
-  EV(0);
+  auto mark = [&](int sl) {
+    if (log) log->mark(sl, st);
+  };
   const bool fx = s->fused_xy != 0;
   if (fx) {
+    mark(0);
     if (!fused_xy(true, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st)) {
       cg_set_error("fused transverse pass launch failed: %s", cudaGetErrorString(cudaGetLastError()));
       return CG_ERR_CUDA;
     }
-    EV(1);
-    EV(2);
   } else {
+    mark(0);
     if (!fast_ypass(Y_FWD, d, t, s->S0, s->S1, s->S2, B, st))
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD, d, s->py, t, s->S0, s->S1, s->S2);
-    EV(1);
+    mark(1);
     if (!fast_xpass(X_GRAD, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
       k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_GRAD, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
-    EV(2);
+    mark(2);
     if (!fast_ypass(Y_INV_GRAD, d, t, s->S0, s->S1, s->S2, B, st))
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
   }
-  EV(3);
+  mark(3);
   if (!fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, s->zpers != 0))
     k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
-  EV(4);
   if (fx) {
+    mark(4);
     if (!fused_xy(false, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st)) {
       cg_set_error("fused transverse pass launch failed: %s", cudaGetErrorString(cudaGetLastError()));
       return CG_ERR_CUDA;
     }
-    EV(5);
-    EV(6);
   } else {
+    mark(4);
     if (!fast_ypass(Y_FWD_DIV, d, t, s->S0, s->S1, s->S2, B, st))
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_FWD_DIV, d, s->py, t, s->S0, s->S1, s->S2);
-    EV(5);
+    mark(5);
     if (!fast_xpass(X_DIV, d, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2, B, st))
       k_xpass<<<gx, CG_THREADS, s->smem_x, st>>>(X_DIV, d, s->px, t, (float)s->kcoef, s->invN, s->S0, s->S1, s->S2);
-    EV(6);
+    mark(6);
     if (!fast_ypass(Y_INV, d, t, s->S0, s->S1, s->S2, B, st))
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
   }
-  EV(7);
+  mark(7);
   if (!fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st,
                     s->zpers != 0))
     k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
                                                  record, s->p, s->S0);
-  EV(8);
-#undef EV
+  if (log) cudaEventRecord(log->ev[log->n], st);
+  return CG_OK;
+}
+
+// The pressure spectrum a step starts from, from the pressure field: its
+// z-transform (every mode), then its y-transform in slab mode.
+static int spectrum_from_pressure(cg_solver* s) {
+  const dim3 gz((unsigned)(s->d.nx * ((s->d.ny + CG_ZROWS - 1) / CG_ZROWS)), s->B);
+  if (!fast_zpass_fwd_step(s->d, make_tables(s), make_medium(s), s->p, s->S0, s->B, s->stream, s->zpers != 0))
+    k_zpass_p<<<gz, CG_THREADS, s->smem_z, s->stream>>>(0, s->d, s->pz, make_tables(s), make_medium(s),
+                                                         make_source(s), make_record(s), s->ctl, 0, 0, s->p, s->S0);
+  if (s->slabs > 1 && !fast_ypass(Y_FWD, s->d, make_tables(s), s->S0, s->S1, s->S2, s->B, s->stream)) {
+    cg_set_error("slab mode without a size-specialised y-pass");
+    return CG_ERR_INVALID;
+  }
+  CG_CUDA_TRY(cudaGetLastError());
   return CG_OK;
 }
 
@@ -1184,12 +1309,8 @@ extern "C" int cg_solver_set_state(cg_solver* s, const float* p, const float* u,
   CG_CUDA_TRY(cudaMemcpyAsync(s->p, p, sizeof(float) * n, cudaMemcpyDefault, s->stream));
   CG_CUDA_TRY(cudaMemcpyAsync(s->u, u, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
   k_set_ctl<<<1, 1, 0, s->stream>>>(s->ctl, step);
-  const dim3 gz((unsigned)(s->d.nx * ((s->d.ny + CG_ZROWS - 1) / CG_ZROWS)), s->B);
-  if (!fast_zpass_p(0, s->d, make_tables(s), make_medium(s), make_source(s), make_record(s), s->ctl, 0, 0, s->p,
-                    s->S0, s->B, s->stream))
-    k_zpass_p<<<gz, CG_THREADS, s->smem_z, s->stream>>>(0, s->d, s->pz, make_tables(s), make_medium(s),
-                                                         make_source(s), make_record(s), s->ctl, 0, 0, s->p, s->S0);
-  CG_CUDA_TRY(cudaGetLastError());
+  const int rc = spectrum_from_pressure(s);
+  if (rc != CG_OK) return rc;
   CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   return CG_OK;
 }
@@ -1222,7 +1343,7 @@ extern "C" int cg_solver_info(const cg_solver* s, long long* out /* 8 */) {
   out[4] = (long long)s->smem_x;
   out[5] = (long long)s->smem_z;
   out[6] = s->B;
-  out[7] = s->fused_xy ? 4 : 8;  // kernel launches per step
+  out[7] = s->slabs > 1 ? 2 + 6 * s->slabs : (s->fused_xy ? 4 : 8);  // kernel launches per step
   return CG_OK;
 }
 
@@ -1262,36 +1383,59 @@ struct TuneKey {
     return false;
   }
 };
-std::map<TuneKey, std::pair<int, int>> g_tuned;
+struct TuneChoice {
+  int fused, zpers, slabs;
+};
+std::map<TuneKey, TuneChoice> g_tuned;
 std::mutex g_tune_mu;
 }  // namespace
+
+// Slab counts the tuner tries: each slab's working set (three spectra,
+// three velocity fields and the labels of its x-planes) between about 20 and
+// 90 MB, so that it stays in L2 between the slab's three passes, capped at
+// CG_MAX_SLABS and at one x-plane per slab.
+static int slab_candidates(const cg_solver* s, int* out) {
+  if (!slabs_supported(s->d)) return 0;
+  const double plane = (double)s->B * ((double)s->d.nzh * s->d.ny * 8.0 * 3.0 + (double)s->d.ny * s->d.nz * 13.0);
+  const double total = plane * s->d.nx;
+  int n = 0;
+  for (int k = 2; k <= CG_MAX_SLABS && k <= s->d.nx; ++k) {
+    const double ws = total / k;
+    if (ws <= 90e6 && ws >= 20e6) out[n++] = k;
+  }
+  return n;
+}
 
 extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   CG_REQUIRE(s && out4, "null argument");
   CG_REQUIRE(s->has_medium, "set a medium before tuning");
   CG_REQUIRE(n_steps >= 1, "n_steps must be >= 1");
   const TuneKey key{s->d.nx, s->d.ny, s->d.nz, s->B, s->nonlinear, s->labels != nullptr};
-  // CG_FUSED_XY=0 / =1 pin the transverse chain (comparison runs): no cache
+  // CG_FUSED_XY=0 / =1 pin the transverse chain and CG_SLABS=k the slab
+  // count (comparison runs): no cache then
   const char* fenv = getenv("CG_FUSED_XY");
-  const bool pinned = fenv && (fenv[0] == '0' || fenv[0] == '1');
+  const char* senv = getenv("CG_SLABS");
+  const bool slab_pinned = senv && senv[0] >= '0' && senv[0] <= '9';
+  const bool pinned = (fenv && (fenv[0] == '0' || fenv[0] == '1')) || slab_pinned;
   if (!pinned) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
       invalidate_graphs(s);
-      s->fused_xy = it->second.first;
-      s->zpers = it->second.second;
+      s->fused_xy = it->second.fused;
+      s->zpers = it->second.zpers;
+      s->slabs = it->second.slabs;
       out4[0] = s->fused_xy;
       out4[1] = s->zpers;
       out4[2] = 0;
       out4[3] = 1;
-      return CG_OK;
+      return cg_solver_reset(s);
     }
   }
-  const bool fx_ok = !(fenv && fenv[0] == '0') && fused_xy_supported(s->d);
+  const bool fx_ok = !(fenv && fenv[0] == '0') && !slab_pinned && fused_xy_supported(s->d);
   const int fx_lo = (fx_ok && fenv && fenv[0] == '1') ? 1 : 0;
   // the per-tile z-passes exist for the lengths of CG_FAST_SIZES only
-  const bool zp_choice = (s->d.ny % 2 == 0) && fast_has(s->d.nz);
+  const bool zp_choice = (s->d.ny % 2 == 0) && fast_has(s->d.nz) && !slab_pinned;
   invalidate_graphs(s);
   cudaEvent_t a, b;
   CG_CUDA_TRY(cudaEventCreate(&a));
@@ -1301,18 +1445,31 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   // process tunes while other solves run) cannot hand the choice to a
   // slower configuration.
   constexpr int kRounds = 3;
-  int cand_fx[4], cand_zp[4], nc = 0;
-  float cand_ms[4];
-  for (int fx = fx_lo; fx <= (fx_ok ? 1 : 0); ++fx)
-    for (int zp = 1; zp >= (zp_choice ? 0 : 1); --zp) {
-      cand_fx[nc] = fx;
-      cand_zp[nc] = zp;
-      cand_ms[nc++] = 1e30f;
+  constexpr int kMaxCand = 4 + CG_MAX_SLABS;
+  TuneChoice cand[kMaxCand];
+  float cand_ms[kMaxCand];
+  int nc = 0;
+  if (slab_pinned) {
+    const int k = atoi(senv);
+    cand[nc++] = {0, 1, (k > 1 && slabs_supported(s->d)) ? (k > CG_MAX_SLABS ? CG_MAX_SLABS : k) : 1};
+  } else {
+    for (int fx = fx_lo; fx <= (fx_ok ? 1 : 0); ++fx)
+      for (int zp = 1; zp >= (zp_choice ? 0 : 1); --zp) cand[nc++] = {fx, zp, 1};
+    // slab counts join the candidates only on request (CG_TUNE_SLABS=1): on
+    // GB300 they measured slower than the plain step on every grid tried
+    const char* tenv = getenv("CG_TUNE_SLABS");
+    if (!(fenv && fenv[0] == '1') && tenv && tenv[0] == '1') {
+      int ks[CG_MAX_SLABS];
+      const int nk = slab_candidates(s, ks);
+      for (int i = 0; i < nk; ++i) cand[nc++] = {0, 1, ks[i]};
     }
+  }
+  for (int c = 0; c < nc; ++c) cand_ms[c] = 1e30f;
   for (int r = 0; r < kRounds; ++r)
     for (int c = 0; c < nc; ++c) {
-      s->fused_xy = cand_fx[c];
-      s->zpers = cand_zp[c];
+      s->fused_xy = cand[c].fused;
+      s->zpers = cand[c].zpers;
+      s->slabs = cand[c].slabs;
       int rc = CG_OK;
       for (int k = 0; k < (r == 0 ? 2 : 1) && rc == CG_OK; ++k) rc = launch_step(s, k % s->spp, 0);
       CG_CUDA_TRY(cudaEventRecord(a, s->stream));
@@ -1328,28 +1485,56 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
       CG_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
       if (ms < cand_ms[c]) cand_ms[c] = ms;
     }
-  float best = 1e30f;
-  int best_fx = 0, best_zp = 1, tried = nc;
+  float best_ms = 1e30f;
+  TuneChoice best = cand[0];
   for (int c = 0; c < nc; ++c)
-    if (cand_ms[c] < best) {
-      best = cand_ms[c];
-      best_fx = cand_fx[c];
-      best_zp = cand_zp[c];
+    if (cand_ms[c] < best_ms) {
+      best_ms = cand_ms[c];
+      best = cand[c];
     }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  s->fused_xy = best_fx;
-  s->zpers = best_zp;
+  s->fused_xy = best.fused;
+  s->zpers = best.zpers;
+  s->slabs = best.slabs;
   int rc = cg_solver_reset(s);
   if (rc != CG_OK) return rc;
   if (!pinned) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tuned[key] = {best_fx, best_zp};
+    g_tuned[key] = best;
   }
-  out4[0] = best_fx;
-  out4[1] = best_zp;
-  out4[2] = tried;
+  out4[0] = best.fused;
+  out4[1] = best.zpers;
+  out4[2] = nc;
   out4[3] = 0;
+  return CG_OK;
+}
+
+extern "C" int cg_solver_set_slabs(cg_solver* s, int slabs) {
+  CG_REQUIRE(s, "null solver");
+  CG_REQUIRE(slabs >= 1 && slabs <= CG_MAX_SLABS, "slabs must lie in [1, %d], got %d", CG_MAX_SLABS, slabs);
+  CG_REQUIRE(slabs == 1 || slabs <= s->d.nx, "%d slabs on %d x-planes", slabs, s->d.nx);
+  CG_REQUIRE(slabs == 1 || slabs_supported(s->d),
+             "slab mode needs size-specialised passes on every axis and an even ny (grid %dx%dx%d)", s->d.nx,
+             s->d.ny, s->d.nz);
+  if (slabs == s->slabs) return CG_OK;
+  invalidate_graphs(s);
+  s->fused_xy = 0;
+  s->zpers = 1;
+  s->slabs = slabs;
+  // the step-start spectrum of the new mode, from the current pressure
+  const int rc = spectrum_from_pressure(s);
+  if (rc != CG_OK) return rc;
+  CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return CG_OK;
+}
+
+extern "C" int cg_solver_get_config(const cg_solver* s, int* out4) {
+  CG_REQUIRE(s && out4, "null argument");
+  out4[0] = s->fused_xy;
+  out4[1] = s->zpers;
+  out4[2] = s->slabs;
+  out4[3] = s->slabs > 1 ? 2 + 6 * s->slabs : (s->fused_xy ? 4 : 8);
   return CG_OK;
 }
 
@@ -1358,22 +1543,25 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
 extern "C" int cg_solver_profile(cg_solver* s, int n_steps, int record, float* ms8) {
   CG_REQUIRE(s && ms8, "null argument");
   CG_REQUIRE(!record || s->bins, "recording needs cg_solver_begin_record first");
-  cudaEvent_t ev[9];
-  for (int i = 0; i < 9; ++i) CG_CUDA_TRY(cudaEventCreate(&ev[i]));
+  EvLog log;
+  for (int i = 0; i < EvLog::kMax; ++i) CG_CUDA_TRY(cudaEventCreate(&log.ev[i]));
   for (int i = 0; i < 8; ++i) ms8[i] = 0.f;
-  for (int k = 0; k < n_steps; ++k) {
-    launch_step(s, k % s->spp, record, ev);
-    CG_CUDA_TRY(cudaEventSynchronize(ev[8]));
-    for (int i = 0; i < 8; ++i) {
+  int rc = CG_OK;
+  for (int k = 0; k < n_steps && rc == CG_OK; ++k) {
+    log.n = 0;
+    rc = launch_step(s, k % s->spp, record, &log);
+    if (rc != CG_OK) break;
+    CG_CUDA_TRY(cudaEventSynchronize(log.ev[log.n]));
+    for (int i = 0; i < log.n; ++i) {
       float t = 0.f;
-      CG_CUDA_TRY(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
-      ms8[i] += t;
+      CG_CUDA_TRY(cudaEventElapsedTime(&t, log.ev[i], log.ev[i + 1]));
+      ms8[log.slot[i]] += t;
     }
   }
   k_advance<<<1, 1, 0, s->stream>>>(s->ctl, n_steps);
-  for (int i = 0; i < 9; ++i) cudaEventDestroy(ev[i]);
+  for (int i = 0; i < EvLog::kMax; ++i) cudaEventDestroy(log.ev[i]);
   CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
-  return CG_OK;
+  return rc;
 }
 
 // ------------------------------------------------ standalone 3-D FFT ----

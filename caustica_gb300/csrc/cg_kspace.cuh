@@ -9,6 +9,7 @@
 #define CG_ZROWS 32  // real rows per z tile (two per complex pencil)
 #define CG_MAX_H 8
 #define CG_THREADS 256
+#define CG_MAX_SLABS 8  // x-slabs of the slab-mode step
 
 enum YMode { Y_FWD = 0, Y_INV = 1, Y_INV_GRAD = 2, Y_FWD_DIV = 3 };
 enum XMode { X_GRAD = 0, X_DIV = 1, X_FWD = 2, X_INV = 3 };
@@ -121,6 +122,12 @@ bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, 
 bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src,
                   const RecordDev& rec, const long long* ctl, int n_local, int record, float* p, float2* S0,
                   int batch, cudaStream_t st, bool persistent = true);
+
+// The forward z-transform of p into S0 with the kernel family the step's
+// p-pass runs on this grid (bitwise the spectrum a step leaves); false when
+// no size-specialised kernel covers nz.
+bool fast_zpass_fwd_step(const Dims& d, const Tables& t, const MediumDev& m, float* p, float2* S0, int batch,
+                         cudaStream_t st, bool persistent);
 
 // Axis lengths with a size-specialised kernel.
 #define CG_FAST_SIZES(X) X(8) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(160) X(192) X(256)

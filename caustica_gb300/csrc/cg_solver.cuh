@@ -40,6 +40,10 @@ struct cg_solver {
   size_t smem_y = 0, smem_x = 0, smem_z = 0;
   int fused_xy = 0;  // the transverse passes run as two cluster launches per step
   int zpers = 1;     // persistent z-passes (where the grid allows)
+  // x-slabs of the plane-local passes: > 1 runs [y, z, y] slab by slab so
+  // each slab's spectra and fields stay in L2 between its three passes; the
+  // pressure spectrum between steps is then y- and z-transformed
+  int slabs = 1;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one period, record off/on
   // phasors of the last finalize, [B][nh][nrec], kept for device post-processing
   float2* ph = nullptr;

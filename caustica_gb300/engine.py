@@ -507,7 +507,9 @@ class DeviceSolver:
             # launch configuration timed on this (fresh) handle, remembered per shape
             out = np.zeros(4, np.int32)
             _lib.call("cg_solver_autotune", h, 4, _lib.ptr(out))
-            self.tuning = {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]),
+            cfg4 = np.zeros(4, np.int32)
+            _lib.call("cg_solver_get_config", h, _lib.ptr(cfg4))
+            self.tuning = {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]), "slabs": int(cfg4[2]),
                            "configurations_timed": int(out[2]), "cached": bool(out[3])}
         info = np.zeros(8, np.int64)
         _lib.call("cg_solver_info", h, _lib.ptr(info))
@@ -523,6 +525,19 @@ class DeviceSolver:
             raise ValueError(f"phases for {ac.shape[0]} members given to a batch of {self.batch}")
         xyz = np.ascontiguousarray(self.plan.src_xyz)
         _lib.call("cg_solver_set_source", self.h, int(xyz.shape[0]), _lib.ptr(xyz), _lib.ptr(ac), _lib.ptr(as_))
+
+    def set_slabs(self, k: int) -> None:
+        """Run the plane-local passes in ``k`` x-slabs (1: the plain step); bit-identical results."""
+        _lib.call("cg_solver_set_slabs", self.h, int(k))
+        info = np.zeros(8, np.int64)
+        _lib.call("cg_solver_info", self.h, _lib.ptr(info))
+        self.launches_per_step = int(info[7])
+
+    def config(self) -> dict:
+        out = np.zeros(4, np.int32)
+        _lib.call("cg_solver_get_config", self.h, _lib.ptr(out))
+        return {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]), "slabs": int(out[2]),
+                "launches_per_step": int(out[3])}
 
     def extend_drive(self, n_steps: int) -> None:
         """Drive table covering ``n_steps`` steps (the default covers one solve's schedule)."""

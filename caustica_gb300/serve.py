@@ -78,14 +78,49 @@ class Outcome:
         return self.t_done - self.t_submit
 
 
+_MEDIA = ("alpha", "rho", "c", "beta")
+_FP_CACHE: dict = {}  # id(medium) -> (medium, fingerprint); holds the object, so its id stays unique
+_FP_STRIDE = 61
+
+
+def medium_fingerprint(medium) -> str:
+    """A content fingerprint of a medium: shape plus a strided sample of its
+    four maps. Equal media always get equal fingerprints; two requests whose
+    fingerprints match share a handle only after :func:`same_medium`
+    compares the whole maps."""
+    hit = _FP_CACHE.get(id(medium))
+    if hit is not None and hit[0] is medium:
+        return hit[1]
+    h = hashlib.sha1()
+    for name in _MEDIA:
+        a = np.ascontiguousarray(getattr(medium, name), np.float32)
+        h.update(str(a.shape).encode())
+        h.update(a.reshape(-1)[::_FP_STRIDE].tobytes())
+    fp = h.hexdigest()
+    _FP_CACHE[id(medium)] = (medium, fp)
+    while len(_FP_CACHE) > 64:
+        _FP_CACHE.pop(next(iter(_FP_CACHE)))
+    return fp
+
+
+def same_medium(a, b) -> bool:
+    """Bitwise equality of two media's maps (the same object trivially)."""
+    if a is b:
+        return True
+    return all(np.array_equal(np.asarray(getattr(a, n), np.float32), np.asarray(getattr(b, n), np.float32))
+               for n in _MEDIA)
+
+
 def _key(req: Request) -> tuple:
-    """Requests with equal keys can share one batched handle."""
+    """Requests with equal keys (and equal media, :func:`same_medium`) can
+    share one batched handle: media are compared by content, so two
+    requests that carry equal media built separately pack as well."""
     src = req.source
     h = hashlib.sha1(np.ascontiguousarray(src.indices).tobytes()).hexdigest()
     spec = req.spec
     sk = tuple(sorted((spec.model_dump() if hasattr(spec, "model_dump") else dict(spec.__dict__)).items()))
     rr = None if req.record_region is None else tuple((s.start, s.stop) for s in req.record_region)
-    return (id(req.medium), tuple(req.grid.shape), req.grid.dx, req.grid.pml_vox, float(src.f0),
+    return (medium_fingerprint(req.medium), tuple(req.grid.shape), req.grid.dx, req.grid.pml_vox, float(src.f0),
             float(src.amplitude), float(src.ramp_periods), h, sk, bool(req.nonlinear), tuple(req.harmonics), rr,
             None if req.reference_point is None else tuple(req.reference_point))
 
@@ -302,8 +337,7 @@ class Server:
     def _plan(self, req: Request):
         k = _key(req)
         hit = self._plans.get(k)
-        # the cache holds the medium object itself, so its id cannot be reused
-        if hit is not None and hit[0] is req.medium:
+        if hit is not None and same_medium(hit[0], req.medium):
             return k, hit[1]
         plan = make_plan("serve_gb300", req.grid, req.medium, req.source, req.spec,
                          record_region=req.record_region, reference_point=req.reference_point,
@@ -331,7 +365,8 @@ class Server:
                 rest = deque()
                 while self._pending and len(items) < self.max_pack:
                     it = self._pending.popleft()
-                    (items if _key(it[0]) == key else rest).append(it)
+                    fits = _key(it[0]) == key and same_medium(it[0].medium, req.medium)
+                    (items if fits else rest).append(it)
                 rest.extend(self._pending)
                 self._pending = rest
             need = device_footprint(plan, len(items))

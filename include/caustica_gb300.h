@@ -115,13 +115,26 @@ int cg_solver_profile(cg_solver* s, int n_steps, int record, float* ms8);
 int cg_solver_info(const cg_solver* s, long long* out8);
 /* Autotuner: on a fresh handle (medium, source and drive set) time each
  * launch configuration the grid admits -- cluster-fused or three-pass
- * transverse chain, persistent or one-tile-per-CTA z-passes -- over
+ * transverse chain, persistent or one-tile-per-CTA z-passes (and slab
+ * counts, cg_solver_set_slabs, when CG_TUNE_SLABS=1) -- over
  * n_steps steps of the handle itself, keep the fastest and reset the
  * handle's state. The choice is remembered per (grid, batch, physics,
  * medium storage) for the process. out4 = {fused, persistent z, configurations
  * timed, 1 when taken from the process cache}. No counterpart in the
  * reference (it has one code path). */
 int cg_solver_autotune(cg_solver* s, int n_steps, int* out4);
+
+/* Run the plane-local passes slab by slab: 1 <= slabs <= 8; 1 is the plain
+ * eight-launch step. With k > 1 slabs a step is x grad, then for each of k
+ * runs of x-planes [y inv grad, z u, y fwd div], x div, then for each run
+ * [y inv, z p, y fwd]: a run's spectra and fields stay in L2 between its
+ * three passes. Results are bit-identical in every mode. Needs the
+ * size-specialised passes on all three axes and an even ny. Synchronises.
+ * No counterpart in the reference (it has one code path). */
+int cg_solver_set_slabs(cg_solver* s, int slabs);
+/* out4 = {cluster-fused transverse chain, persistent z-passes, slabs,
+ * kernel launches per step} of the handle's current launch configuration. */
+int cg_solver_get_config(const cg_solver* s, int* out4);
 
 /* ------------------------------------------------- batched 3-D R2C/C2R */
 

@@ -133,3 +133,44 @@ def test_server_admits_by_budget_and_still_finishes_everything():
         outs = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
         assert srv.stats["max_active"] == 1
     assert len(outs) == 4
+
+
+def test_requests_arriving_while_the_gpu_is_busy_pack_across_arrivals():
+    """A long request holds the whole budget; three compatible requests that
+    arrive one after another while it runs (their media equal in content but
+    built separately) wait, are packed into one handle when memory frees,
+    and each result equals its solo solve."""
+    import time
+
+    spec_long = cg.CWRunSpec(convergence_tol=0.0, min_settle_periods=40, max_settle_periods=40, n_record_periods=2)
+    grid_l, med_l, idx_l, _ = _setup((64, 64, 96), 21)
+    src_l = cg.CWSource(indices=idx_l, phases=np.zeros(len(idx_l), np.float32), amplitude=2e5, f0=1e6)
+    long_req = serve.Request(grid=grid_l, medium=med_l, source=src_l, spec=spec_long, tag="long")
+    spec = cg.CWRunSpec(convergence_tol=0.0, min_settle_periods=2, max_settle_periods=3, n_record_periods=2)
+    late = []
+    for k in range(3):
+        grid, med, idx, rng = _setup((16, 24, 32), 22)  # same seed: equal media, distinct objects
+        ph = np.random.default_rng(100 + k).uniform(0, 2 * np.pi, len(idx)).astype(np.float32)
+        late.append(serve.Request(grid=grid, medium=med, source=cg.CWSource(indices=idx, phases=ph, amplitude=2e5,
+                                                                            f0=1e6), spec=spec, tag=("late", k)))
+    assert late[0].medium is not late[1].medium
+    from caustica_gb300.engine import device_footprint, make_plan
+
+    plan_l = make_plan("x", grid_l, med_l, src_l, spec_long)
+    plan_s = make_plan("x", late[0].grid, late[0].medium, late[0].source, spec)
+    # room for the long request or the packed three, never for the long one and any other
+    budget = max(device_footprint(plan_l, 1), device_footprint(plan_s, 3))
+    assert budget < device_footprint(plan_l, 1) + device_footprint(plan_s, 1)
+    with serve.Server(hbm_budget_bytes=budget, max_pack=8) as srv:
+        futs = [srv.submit(long_req)]
+        for r in late:
+            time.sleep(0.002)
+            futs.append(srv.submit(r))
+        outs = [f.result(timeout=300) for f in futs]
+        stats = dict(srv.stats)
+    assert stats["groups"] == 2, stats
+    assert [o.group_size for o in outs[1:]] == [3, 3, 3]
+    assert outs[1].t_admit >= outs[0].t_done - 1e-3  # admitted once the long request released its memory
+    for r, o in zip(late, outs[1:]):
+        solo = _solo(r.grid, r.medium, r.source.indices, r.source.phases, r.spec, False)
+        assert rel_l2(o.result.phasor, solo.phasor) < 1e-6, r.tag

@@ -48,7 +48,24 @@ def _setup_3d_westervelt():
     return grid, med, src, spec, cg.WesterveltKSpaceGB300(), (1, 2)
 
 
-SETUPS = {"linear_1d": _setup_1d, "westervelt_3d": _setup_3d_westervelt}
+def _setup_3d_size_specialised():
+    """A grid whose every axis runs the size-specialised passes (persistent
+    z-passes): the restored spectrum must come from the step's own kernel."""
+    rng = np.random.default_rng(23)
+    shape = (32, 48, 64)
+    dx = 0.2e-3
+    grid = cg.Grid(shape, dx, cg.PMLSpec(3 * dx))
+    labels = rng.integers(0, 3, shape)
+    table = {0: (2.5, 1000.0, 1500.0, 3.5), 1: (8.0, 1050.0, 1580.0, 4.7), 2: (20.0, 1090.0, 1610.0, 4.95)}
+    med = cg.Medium.from_labels(labels, table)
+    idx = np.array([[16, 24, 5], [16, 25, 5], [15, 24, 5], [17, 23, 6], [16, 24, 6]])
+    src = cg.CWSource(indices=idx, phases=rng.uniform(-1, 1, len(idx)).astype(np.float32), amplitude=1.2e6, f0=F0)
+    spec = cg.CWRunSpec(min_settle_periods=3, max_settle_periods=9, convergence_tol=0.005, n_record_periods=2)
+    return grid, med, src, spec, cg.WesterveltKSpaceGB300(), (1, 2)
+
+
+SETUPS = {"linear_1d": _setup_1d, "westervelt_3d": _setup_3d_westervelt,
+          "westervelt_3d_size_specialised": _setup_3d_size_specialised}
 
 
 def _stop_after(k: int):
