@@ -792,19 +792,6 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const bool conv_b = x_conv && yb >= rec.clo[1] && yb < rec.chi[1];
     const bool rec_a = x_rec && ya >= rec.lo[1] && ya < rec.hi[1];
     const bool rec_b = x_rec && yb >= rec.lo[1] && yb < rec.hi[1];
-    float* bins = rec.bins + (b_idx * rec.spp + m_bin) * rec.nrec;
-    float* comp = rec.comp + (b_idx * rec.spp + m_bin) * rec.nrec;
-    float* pmax = rec.pmax + b_idx * rec.nrec;
-    auto record_cell = [&](int y, int n, float pn, float apn) {
-      const long long ri = ((long long)(x - rec.lo[0]) * Ry + (y - rec.lo[1])) * Rz + (n - rec.lo[2]);
-      const float sv = bins[ri], cm0 = comp[ri];
-      const float yk = pn - cm0;
-      const float tk = sv + yk;
-      comp[ri] = (tk - sv) - yk;
-      bins[ri] = tk;
-      const float pm = pmax[ri];
-      pmax[ri] = (apn > pm || apn != apn) ? apn : pm;
-    };
     if (s < A) static_for<0, B>([&](auto bi) {
       constexpr int b = decltype(bi)::value;
       const int n = s + A * b;
@@ -813,16 +800,57 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
         pb[rowa + n] = pna;
         pb[rowb + n] = pnb;
       }
-      const float apa = fabsf(pna), apb = fabsf(pnb);
       if ((zconv >> b) & 1u) {
-        if (conv_a) lpeak = max(lpeak, __float_as_uint(apa));
-        if (conv_b) lpeak = max(lpeak, __float_as_uint(apb));
-      }
-      if (REC && ((zrec >> b) & 1u)) {
-        if (rec_a) record_cell(ya, n, pna, apa);
-        if (rec_b) record_cell(yb, n, pnb, apb);
+        if (conv_a) lpeak = max(lpeak, __float_as_uint(fabsf(pna)));
+        if (conv_b) lpeak = max(lpeak, __float_as_uint(fabsf(pnb)));
       }
     });
+    if constexpr (REC) {
+      // phase bin m (Kahan-compensated sum) and running max |p| of this
+      // thread's recorded cells, RC cells per row at a time: every load of a
+      // chunk is issued before its first store, so the chunk costs one round
+      // trip to memory instead of one per cell
+      if (s < A && (rec_a || rec_b)) {
+        float* __restrict__ bins = rec.bins + (b_idx * rec.spp + m_bin) * rec.nrec;
+        float* __restrict__ comp = rec.comp + (b_idx * rec.spp + m_bin) * rec.nrec;
+        float* __restrict__ pmax = rec.pmax + b_idx * rec.nrec;
+        const long long ra = ((long long)(x - rec.lo[0]) * Ry + (ya - rec.lo[1])) * Rz - rec.lo[2];
+        const long long rb = ra + Rz;  // row yb = ya + 1
+        constexpr int RC = 4;
+        static_assert(B % RC == 0, "record chunks split the thread's cells evenly");
+        static_for<0, B / RC>([&](auto ci) {
+          constexpr int c0 = decltype(ci)::value * RC;
+          float sv[2 * RC], cm[2 * RC], pm[2 * RC];
+          static_for<0, RC>([&](auto ji) {
+            constexpr int j = decltype(ji)::value, b = c0 + j;
+            const int n = s + A * b;
+            const bool in = (zrec >> b) & 1u;
+            sv[j] = (in && rec_a) ? bins[ra + n] : 0.f;
+            cm[j] = (in && rec_a) ? comp[ra + n] : 0.f;
+            pm[j] = (in && rec_a) ? pmax[ra + n] : 0.f;
+            sv[RC + j] = (in && rec_b) ? bins[rb + n] : 0.f;
+            cm[RC + j] = (in && rec_b) ? comp[rb + n] : 0.f;
+            pm[RC + j] = (in && rec_b) ? pmax[rb + n] : 0.f;
+          });
+          static_for<0, RC>([&](auto ji) {
+            constexpr int j = decltype(ji)::value, b = c0 + j;
+            const int n = s + A * b;
+            if (!((zrec >> b) & 1u)) return;
+            for (int r = 0; r < 2; ++r) {
+              if (r ? !rec_b : !rec_a) continue;
+              const long long ri = (r ? rb : ra) + n;
+              const float pn = r ? w[b].y : w[b].x, apn = fabsf(pn);
+              const int k = r * RC + j;
+              const float yk = pn - cm[k];
+              const float tk = sv[k] + yk;
+              comp[ri] = (tk - sv[k]) - yk;
+              bins[ri] = tk;
+              pmax[ri] = (apn > pm[k] || apn != apn) ? apn : pm[k];
+            }
+          });
+        });
+      }
+    }
     lpeak = __reduce_max_sync(0xffffffffu, lpeak);
     if ((threadIdx.x & 31) == 0 && lpeak) atomicMax(&s_peak, lpeak);
     __syncthreads();
