@@ -133,6 +133,9 @@ SIGNATURES = {
     "cg_solver_focus_metrics": [_P, _I, C.POINTER(FocusInput), C.POINTER(FocusReport)],
     "cg_heating_q": [C.POINTER(HeatingSpec), _P, _P, _P],
     "cg_solver_heating_q": [_P, _I, C.POINTER(HeatingSpec), _P, _P],
+    "cg_label_counts": [_P, _LL, _P],
+    "cg_gather_u8": [_P, _P, _I, _P],
+    "cg_stream_synchronize": [_P],
     "cg_buffer_alloc": [C.c_size_t, C.POINTER(_P)],
     "cg_buffer_free": [_P],
     "cg_buffer_copy": [_P, _P, C.c_size_t],

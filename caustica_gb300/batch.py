@@ -21,7 +21,13 @@ def solve_steering(grid, medium, indices, phases, *, f0: float, amplitude: float
                    nonlinear: bool = False, harmonics=(1,), record_region=None, reference_point=None,
                    ramp_periods: float = 3.0, max_batch: int | None = None, name: str = "steering_gb300",
                    result_cls=SolverResult) -> list:
-    """Solve B steering positions; ``phases`` is (B, n_voxels) float32."""
+    """Solve B steering positions; ``phases`` is (B, n_voxels) float32, host
+    or device (a device array is read back: the source scale is formed with
+    the host's float32 arithmetic either way)."""
+    from .device import is_device_array, to_host
+
+    if is_device_array(phases):
+        phases = to_host(phases, np.float32)
     phases = np.ascontiguousarray(np.atleast_2d(np.asarray(phases, np.float32)))
     indices = np.asarray(indices, np.int64)
     if phases.shape[1] != indices.shape[0]:

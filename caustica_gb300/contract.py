@@ -100,10 +100,20 @@ class Medium:
         """Dense volumes from an integer id map and ``{id: (alpha, rho, c, beta)}``
         (the shape of ``Medium.from_id_map``, medium.py:57-81)."""
         id_map = np.asarray(id_map)
-        present = np.unique(id_map)
+        small = id_map.dtype.kind in "iu" and id_map.size > 0 and 0 <= int(id_map.min()) and int(id_map.max()) < 65536
+        if small:  # one gather per property through a lookup table
+            present = np.flatnonzero(np.bincount(id_map.reshape(-1)))
+        else:
+            present = np.unique(id_map)
         unknown = [int(i) for i in present if int(i) not in table]
         if unknown:
             raise ValueError(f"id_map contains ids {unknown} that are missing from the table")
+        if small:
+            lut = np.zeros((int(present[-1]) + 1, 4), np.float32)
+            for i in present:
+                lut[int(i)] = np.asarray(table[int(i)], np.float32)
+            out = [np.ascontiguousarray(lut[:, k])[id_map] for k in range(4)]
+            return cls(*out, id_map=id_map)
         out = [np.zeros(id_map.shape, np.float32) for _ in range(4)]
         for i in present:
             mask = id_map == i
@@ -148,7 +158,14 @@ class CWSource:
 
     def __post_init__(self) -> None:
         idx = np.asarray(self.indices)
-        ph = np.asarray(self.phases, dtype=np.float32)
+        ph = self.phases
+        if not isinstance(ph, np.ndarray) and (hasattr(ph, "__cuda_array_interface__") or
+                                                hasattr(ph, "__dlpack_device__")):
+            from .device import is_device_array, to_host
+
+            if is_device_array(ph):  # device phases: a few KB read back
+                ph = to_host(ph, np.float32)
+        ph = np.asarray(ph, dtype=np.float32)
         if idx.ndim != 2:
             raise ValueError(f"indices must be (n, ndim), got shape {idx.shape}")
         if not np.issubdtype(idx.dtype, np.integer):

@@ -1420,6 +1420,10 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   if (!pinned) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
+    // a batch runs the same kernels with one grid dimension per member: it
+    // takes the choice made for one member on this grid when there is one
+    if (it == g_tuned.end() && key.B > 1) it = g_tuned.find(TuneKey{key.nx, key.ny, key.nz, 1, key.nonlinear,
+                                                                    key.labels});
     if (it != g_tuned.end()) {
       invalidate_graphs(s);
       s->fused_xy = it->second.fused;

@@ -575,3 +575,71 @@ extern "C" int cg_buffer_copy(void* dst, const void* src, size_t bytes) {
   CG_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
   return CG_OK;
 }
+
+// ----------------------------------------- device-resident label volumes --
+// Callers that keep a medium's label map on the device (a framework tensor
+// passed by pointer) still need two small facts on the host: which labels
+// occur (the time step follows the fastest material present) and the labels
+// of the source voxels (the injection scale uses the local sound speed).
+
+__global__ void k_label_counts(const uint8_t* __restrict__ lab, long long n, unsigned long long* counts) {
+  __shared__ unsigned int h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&h[lab[i]], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i]) atomicAdd(&counts[i], (unsigned long long)h[i]);
+}
+
+__global__ void k_gather_u8(const uint8_t* __restrict__ src, const long long* __restrict__ idx, int n,
+                            uint8_t* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = src[idx[i]];
+}
+
+extern "C" int cg_label_counts(const uint8_t* labels_dev, long long n, unsigned long long* counts256) {
+  CG_REQUIRE(labels_dev && counts256, "null argument");
+  CG_REQUIRE(n >= 0, "negative length");
+  cudaPointerAttributes at;
+  CG_CUDA_TRY(cudaPointerGetAttributes(&at, labels_dev));
+  CG_REQUIRE(at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged,
+             "the label volume must be device memory");
+  unsigned long long* d = nullptr;
+  CG_CUDA_TRY(cudaMalloc(&d, 256 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 256 * sizeof(unsigned long long));
+  if (e == cudaSuccess && n > 0) {
+    const long long blocks = (n + 255) / 256;
+    k_label_counts<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256>>>(labels_dev, n, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(counts256, d, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CG_CUDA_TRY(e);
+  return CG_OK;
+}
+
+extern "C" int cg_gather_u8(const uint8_t* src_dev, const long long* idx, int n, uint8_t* out_host) {
+  CG_REQUIRE(src_dev && (n == 0 || (idx && out_host)), "null argument");
+  CG_REQUIRE(n >= 0, "negative count");
+  if (n == 0) return CG_OK;
+  long long* di = nullptr;
+  uint8_t* dout = nullptr;
+  CG_CUDA_TRY(cudaMalloc(&di, sizeof(long long) * n));
+  cudaError_t e = cudaMalloc(&dout, n);
+  if (e == cudaSuccess) e = cudaMemcpy(di, idx, sizeof(long long) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_gather_u8<<<(n + 255) / 256, 256>>>(src_dev, di, n, dout);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out_host, dout, n, cudaMemcpyDeviceToHost);
+  cudaFree(di);
+  if (dout) cudaFree(dout);
+  CG_CUDA_TRY(e);
+  return CG_OK;
+}
+
+extern "C" int cg_stream_synchronize(void* stream) {
+  CG_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return CG_OK;
+}

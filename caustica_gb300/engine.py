@@ -326,6 +326,7 @@ class Plan:
     labels: np.ndarray | None = None
     label_table: np.ndarray | None = None
     label_props: np.ndarray | None = None  # (n, 4) float32 alpha, rho, c, beta per label
+    labels_dev: object | None = None  # device label map (a device.DeviceView) instead of host labels
     dense: tuple | None = None
     label: str = ""
     meta: dict = field(default_factory=dict)
@@ -384,8 +385,9 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
             raise ValueError(f"reference_point must be integer VOXEL indices inside {shape}, "
                              f"got {reference_point} (did you pass meters?)")
     dx = float(grid.dx)
-    c_max = float(np.max(medium.c))
-    c_min = float(np.min(medium.c))
+    device_medium = hasattr(medium, "labels_at")  # a device.DeviceLabelMedium
+    c_max = medium.c_max if device_medium else float(np.max(medium.c))
+    c_min = medium.c_min if device_medium else float(np.min(medium.c))
     spp, dt = cw_discretization(dx, c_max, source.f0, spec, harmonics)
     padded = pad_shape(shape)
     padded3 = _embed3(padded)
@@ -397,6 +399,11 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
         if 2 * pml_vox > n:
             raise ValueError(f"sponge width {pml_vox} does not fit twice into length {n}")
     pml3 = (0,) * (3 - nd) + (pml_vox,) * nd
+    if device_medium:
+        return _device_medium_plan(name, grid, medium, source, spec, record_region=record_region,
+                                   reference_point=reference_point, nonlinear=nonlinear, harmonics=harmonics,
+                                   shape=shape, padded=padded, padded3=padded3, dx=dx, spp=spp, dt=dt,
+                                   c_max=c_max, c_min=c_min, pml3=pml3, pml_edge=pml_edge, pml_vox=pml_vox)
     beta = np.asarray(medium.beta, np.float32)
     nonlinear_active = bool(nonlinear) and not bool((beta == 0).all())
 
@@ -418,6 +425,45 @@ def make_plan(name, grid, medium, source, spec, *, record_region=None, reference
 
     idx = np.asarray(source.indices, np.int64)
     c_src = np.asarray(medium.c, np.float32)[tuple(idx[:, d] for d in range(nd))]
+    return _finish_plan(name, grid, source, spec, record_region=record_region, reference_point=reference_point,
+                        harmonics=harmonics, shape=shape, padded=padded, padded3=padded3, dx=dx, spp=spp, dt=dt,
+                        c_max=c_max, c_min=c_min, pml3=pml3, pml_edge=pml_edge, pml_vox=pml_vox,
+                        nonlinear_active=nonlinear_active, idx=idx, c_src=c_src, labels=labels, table=table,
+                        props=props, dense=dense)
+
+
+def _device_medium_plan(name, grid, medium, source, spec, *, record_region, reference_point, nonlinear, harmonics,
+                        shape, padded, padded3, dx, spp, dt, c_max, c_min, pml3, pml_edge, pml_vox) -> "Plan":
+    """Plan over a label map that stays on the device (device.DeviceLabelMedium):
+    the per-label coefficient table is formed on the host from the rows of
+    the labels that occur, and the map itself goes device to device into the
+    solver."""
+    if tuple(padded) != tuple(shape):
+        raise ValueError(f"a device label map needs a 2/3/5-smooth grid (got {shape}, the FFT size would be "
+                         f"{padded}); pad it on the device first")
+    nonlinear_active = bool(nonlinear) and not medium.is_linear
+    present = medium.present
+    n_lab = int(present.max()) + 1
+    rows = np.array(medium.rows[:n_lab], np.float32)
+    rows[np.setdiff1d(np.arange(n_lab), present)] = rows[present[0]]  # absent labels: any valid row
+    dtr, rc2, ab, b2 = material_coefficients(rows[:, 0], rows[:, 1], rows[:, 2], rows[:, 3], dt, nonlinear_active)
+    table = np.ascontiguousarray(np.stack([dtr, rc2, ab, b2], axis=1).astype(np.float32))
+    idx = np.asarray(source.indices, np.int64)
+    c_src = rows[medium.labels_at(idx).astype(np.int64), 2]
+    plan = _finish_plan(name, grid, source, spec, record_region=record_region, reference_point=reference_point,
+                        harmonics=harmonics, shape=shape, padded=padded, padded3=padded3, dx=dx, spp=spp, dt=dt,
+                        c_max=c_max, c_min=c_min, pml3=pml3, pml_edge=pml_edge, pml_vox=pml_vox,
+                        nonlinear_active=nonlinear_active, idx=idx, c_src=c_src, labels=None, table=table,
+                        props=rows, dense=None)
+    plan.labels_dev = medium.labels
+    plan.meta["present_labels"] = present
+    return plan
+
+
+def _finish_plan(name, grid, source, spec, *, record_region, reference_point, harmonics, shape, padded, padded3,
+                 dx, spp, dt, c_max, c_min, pml3, pml_edge, pml_vox, nonlinear_active, idx, c_src, labels, table,
+                 props, dense) -> "Plan":
+    nd = len(shape)
     src_scale = np.asarray(2.0 * c_src.astype(np.float64) * dt / dx, dtype=np.float32)
     src_xyz = np.zeros((idx.shape[0], 3), np.int32)
     src_xyz[:, 3 - nd:] = idx
@@ -456,7 +502,7 @@ def device_footprint(plan: "Plan", batch: int) -> int:
     nspec = nx * (nz // 2 + 1) * ny
     nrec = int(np.prod([h - l for l, h in zip(plan.rec_lo, plan.rec_hi)]))
     per_member = 16 * ncell + 24 * nspec + 8 * plan.spp * nrec + 4 * nrec + 8 * len(plan.harmonics) * nrec
-    medium = ncell if plan.labels is not None else 16 * ncell
+    medium = ncell if (plan.labels is not None or plan.labels_dev is not None) else 16 * ncell
     return batch * per_member + medium + 16 * plan.max_periods * plan.spp + (64 << 10)
 
 
@@ -487,7 +533,10 @@ class DeviceSolver:
         _lib.check(lib.cg_solver_create(C.byref(cfg), C.byref(h)), "cg_solver_create")
         self.h = h
         try:
-            if plan.labels is not None:
+            if plan.labels_dev is not None:  # device label map: copied device to device
+                _lib.call("cg_solver_set_medium_labels", h, plan.labels_dev.ptr, len(plan.label_table),
+                          _lib.ptr(plan.label_table))
+            elif plan.labels is not None:
                 _lib.call("cg_solver_set_medium_labels", h, _lib.ptr(plan.labels), len(plan.label_table),
                           _lib.ptr(plan.label_table))
             else:
@@ -506,7 +555,8 @@ class DeviceSolver:
         if autotune:
             # launch configuration timed on this (fresh) handle, remembered per shape
             out = np.zeros(4, np.int32)
-            _lib.call("cg_solver_autotune", h, 4, _lib.ptr(out))
+            # a large batch's step is long enough to time in one step per trial
+            _lib.call("cg_solver_autotune", h, 4 if self.batch < 8 else 1, _lib.ptr(out))
             cfg4 = np.zeros(4, np.int32)
             _lib.call("cg_solver_get_config", h, _lib.ptr(cfg4))
             self.tuning = {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]), "slabs": int(cfg4[2]),
@@ -798,7 +848,7 @@ def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result
                           meta={"solver": plan.name, "backend": "gb300", "padded_shape": plan.padded,
                                 "c_ref": plan.c_max, "nonlinear_active": plan.nonlinear_active,
                                 "source": plan.label,
-                                "medium_storage": "labels" if plan.labels is not None else "dense",
+                                "medium_storage": "dense" if plan.dense is not None else "labels",
                                 "batch": batch, "member": b})
             results.append(_results(plan, dev, ph, pm, common, b, result_cls))
     finally:

@@ -339,9 +339,13 @@ class HeatingSource:
         region = tuple(slice(*sl.indices(g)[:2]) for sl, g in zip(result.region, grid))
         region3 = _embed3_region(region, grid)
         props = plan.label_props
-        if plan.labels is not None and props is not None and alpha_at_harmonics is None:
-            sub = (slice(None),) * (3 - len(grid)) + region
-            present = np.flatnonzero(np.bincount(plan.labels[sub].reshape(-1), minlength=256))
+        labelled = plan.labels is not None or plan.labels_dev is not None
+        if labelled and props is not None and alpha_at_harmonics is None:
+            if plan.labels is not None:
+                sub = (slice(None),) * (3 - len(grid)) + region
+                present = np.flatnonzero(np.bincount(plan.labels[sub].reshape(-1), minlength=256))
+            else:  # a device label map: the labels counted over the whole grid (a superset of the region's)
+                present = np.asarray(plan.meta["present_labels"])
             pr = np.asarray(props, np.float64)
             alpha_l, rho_l, c_l = _check_maps(pr[present, 0], pr[present, 1], pr[present, 2], (len(present),))
             alpha_by_h, factors = _resolve_alpha(requested, np.asarray(pr[:, 0]), available=available,

@@ -42,6 +42,7 @@ from typing import Any
 
 import numpy as np
 
+from ._lib import DeviceArray
 from .contract import CWRunSpec
 from .engine import DeviceSolver, _guard_finite, _results, device_footprint, make_plan, member_schedule
 
@@ -114,7 +115,17 @@ def same_medium(a, b) -> bool:
 def _key(req: Request) -> tuple:
     """Requests with equal keys (and equal media, :func:`same_medium`) can
     share one batched handle: media are compared by content, so two
-    requests that carry equal media built separately pack as well."""
+    requests that carry equal media built separately pack as well. The key
+    is kept on the request after its first use."""
+    cached = req.__dict__.get("_cg_key")
+    if cached is not None:
+        return cached
+    key = _make_key(req)
+    req.__dict__["_cg_key"] = key
+    return key
+
+
+def _make_key(req: Request) -> tuple:
     src = req.source
     h = hashlib.sha1(np.ascontiguousarray(src.indices).tobytes()).hexdigest()
     spec = req.spec
@@ -286,11 +297,21 @@ class Server:
     """Continuous-batching CW solve server on one GPU."""
 
     def __init__(self, hbm_budget_bytes: int | None = None, max_pack: int = 8, poll_s: float = 2e-4,
-                 thermal_workers: int = 3):
+                 thermal_workers: int = 3, max_active: int = 6, plan_workers: int = 4):
         if hbm_budget_bytes is None:
             hbm_budget_bytes = 200 << 30
         self.budget = int(hbm_budget_bytes)
         self.max_pack = int(max_pack)
+        # solver handles advancing at once: a few keep the GPU busy; many more
+        # only time-slice it and spread each request's latency
+        self.max_active = max(1, int(max_active))
+        # host set-up of a request (its plan: labels, tables, drive) runs on a
+        # small pool as soon as it is submitted, off the scheduler thread
+        from concurrent.futures import ThreadPoolExecutor
+
+        self._planner = ThreadPoolExecutor(max(1, int(plan_workers)), thread_name_prefix="cg-plan")
+        self._planning: dict = {}
+        self._plans_lock = threading.Lock()
         self.poll_s = float(poll_s)
         self._pending: deque = deque()
         self._lock = threading.Condition()
@@ -299,7 +320,8 @@ class Server:
         self._in_use = 0
         self._plans: dict = {}
         self._thermal_q: queue.Queue = queue.Queue()
-        self.stats = {"groups": 0, "packed_members": 0, "solo_reruns": 0, "peak_bytes": 0, "max_active": 0}
+        self.stats = {"groups": 0, "packed_members": 0, "packed_in_groups": 0, "solo_reruns": 0, "peak_bytes": 0,
+                      "max_active": 0}
         self._thread = threading.Thread(target=self._loop, name="cg-serve", daemon=True)
         # thermal phases run on their own handles and streams, so several overlap on the GPU
         self._tworkers = [threading.Thread(target=self._thermal_loop, name=f"cg-thermal-{i}", daemon=True)
@@ -311,8 +333,10 @@ class Server:
     # -------------------------------------------------------------- api --
     def submit(self, req: Request) -> Future:
         fut: Future = Future()
+        ts = time.perf_counter()
         with self._lock:
-            self._pending.append((req, fut, time.perf_counter()))
+            self._planning[id(req)] = self._planner.submit(self._plan, req)
+            self._pending.append((req, fut, ts))
             self._lock.notify()
         return fut
 
@@ -326,6 +350,7 @@ class Server:
                 self._thermal_q.put(None)
             for t in self._tworkers:
                 t.join()
+            self._planner.shutdown(wait=True)
 
     def __enter__(self):
         return self
@@ -336,28 +361,40 @@ class Server:
     # ------------------------------------------------------------ worker --
     def _plan(self, req: Request):
         k = _key(req)
-        hit = self._plans.get(k)
+        with self._plans_lock:
+            hit = self._plans.get(k)
         if hit is not None and same_medium(hit[0], req.medium):
             return k, hit[1]
         plan = make_plan("serve_gb300", req.grid, req.medium, req.source, req.spec,
                          record_region=req.record_region, reference_point=req.reference_point,
                          nonlinear=req.nonlinear, harmonics=req.harmonics)
-        self._plans[k] = (req.medium, plan)
-        if len(self._plans) > 32:
-            self._plans.pop(next(iter(self._plans)))
+        if plan.labels is not None and plan.labels_dev is None:
+            # the medium's label map stays on the device with the cached plan:
+            # every handle built from it copies device to device
+            plan.labels_dev = DeviceArray.from_host(plan.labels)
+        with self._plans_lock:
+            self._plans[k] = (req.medium, plan)
+            if len(self._plans) > 32:
+                self._plans.pop(next(iter(self._plans)))
         return k, plan
 
     def _admit(self) -> None:
         while True:
+            if len(self._active) >= self.max_active:
+                return  # every slot busy: wait for one to finish
             with self._lock:
                 if not self._pending:
                     return
                 req, fut, ts = self._pending[0]
+                pf = self._planning.get(id(req))
+            if pf is not None and not pf.done():
+                return  # the head request's host set-up is still running
             try:
-                key, plan = self._plan(req)
+                key, plan = pf.result() if pf is not None else self._plan(req)
             except Exception as exc:  # noqa: BLE001 - a bad request fails alone
                 with self._lock:
                     self._pending.popleft()
+                    self._planning.pop(id(req), None)
                 fut.set_exception(exc)
                 continue
             with self._lock:
@@ -369,6 +406,10 @@ class Server:
                     (items if fits else rest).append(it)
                 rest.extend(self._pending)
                 self._pending = rest
+                for it in items:  # members share the head's plan
+                    done = self._planning.pop(id(it[0]), None)
+                    if done is not None and it[0] is not req:
+                        done.cancel()
             need = device_footprint(plan, len(items))
             while len(items) > 1 and self._in_use + need > self.budget:
                 with self._lock:
@@ -389,6 +430,8 @@ class Server:
             self._in_use += g.bytes
             self.stats["groups"] += 1
             self.stats["packed_members"] += len(items)
+            if len(items) > 1:
+                self.stats["packed_in_groups"] += len(items)
             self.stats["peak_bytes"] = max(self.stats["peak_bytes"], self._in_use)
             self.stats["max_active"] = max(self.stats["max_active"], len(self._active))
 
@@ -405,7 +448,7 @@ class Server:
         for b, ((req, fut, ts), out) in enumerate(zip(g.items, results)):
             if out is None:
                 self.stats["solo_reruns"] += 1
-                solo_req = Request(**{**req.__dict__})
+                solo_req = Request(**{k: v for k, v in req.__dict__.items() if not k.startswith("_")})
                 with self._lock:
                     self._pending.appendleft((solo_req, fut, ts))
                 continue

@@ -22,10 +22,13 @@ from typing import Any
 import numpy as np
 
 from . import _lib
+from .device import as_device, is_device_array
 
 
 def _qptr(q):
-    """Host or device pointer of the heating term (the library copies either)."""
+    """Host or device pointer of a field (the library copies either); None -> NULL."""
+    if q is None:
+        return None
     return q.ptr if isinstance(q, _lib.DeviceArray) else _lib.ptr(q)
 
 
@@ -280,8 +283,10 @@ class PennesSolverGB300:
         if q is None:
             return None, "none"
         shape = medium.shape
-        if isinstance(q, _lib.DeviceArray):
-            # Q already on the device (cg_solver_heating_q / cg_heating_q)
+        if is_device_array(q):
+            # Q already on the device (cg_solver_heating_q / cg_heating_q, or a
+            # framework tensor by DLPack / __cuda_array_interface__)
+            q = as_device(q, what="Q")
             if q.shape != tuple(shape) or q.dtype != np.float32:
                 raise ValueError(f"device Q is {q.dtype}{q.shape} but the thermal medium is float32{shape}.")
             return q, "device"
@@ -337,7 +342,9 @@ class PennesSolverGB300:
         t_ref = np.float32(self.reference_temperature_c)
         # theta = T0 - t_ref, its finiteness check (pennes.py:531-536) and
         # T = theta + t_ref on the way out run on the device
-        temp0 = np.ascontiguousarray(temperature0, dtype=np.float32)
+        # a device T0 / dose0 (either exchange protocol) goes to the device calls as it is
+        temp0 = (as_device(temperature0, dtype=np.float32, shape=shape, what="temperature0")
+                 if is_device_array(temperature0) else np.ascontiguousarray(temperature0, dtype=np.float32))
         q_arr, q_kind = self._prepare_q(q, medium)
         ref_minus_ta = np.float32(self.reference_temperature_c - self.arterial_temperature_c)
         theta_wall = np.float32(self.boundary_temperature_c) - t_ref
@@ -378,8 +385,11 @@ class PennesSolverGB300:
                            if perfused and float(ref_minus_ta) != 0.0 else None)
         dose_arr = None
         if dose:
-            dose_arr = (np.zeros(shape, np.float32) if dose0 is None
-                        else np.ascontiguousarray(np.asarray(dose0, np.float32)))
+            if dose0 is not None and is_device_array(dose0):
+                dose_arr = as_device(dose0, dtype=np.float32, shape=shape, what="dose0")
+            else:
+                dose_arr = (np.zeros(shape, np.float32) if dose0 is None
+                            else np.ascontiguousarray(np.asarray(dose0, np.float32)))
             if dose_arr.shape != shape:
                 raise ValueError(f"dose0 has shape {dose_arr.shape} but the medium is {shape}.")
 
@@ -425,7 +435,7 @@ class PennesSolverGB300:
                           _lib.ptr(np.ascontiguousarray(coeff)), _qptr(q_arr),
                           _lib.ptr(np.ascontiguousarray(perf_offset)) if perf_offset is not None else None)
             fin = C.c_int(0)
-            _lib.call("cg_pennes_set_temperature", h, _lib.ptr(temp0), _lib.ptr(dose_arr), C.byref(fin))
+            _lib.call("cg_pennes_set_temperature", h, _qptr(temp0), _qptr(dose_arr), C.byref(fin))
             if not fin.value:
                 raise ValueError("temperature0 contains non-finite values; a solve cannot start from a field that "
                                  "is not a temperature.")

@@ -257,7 +257,7 @@ CONFIG5_GRIDS = ((64, 64, 64), (96, 96, 128), (128, 128, 160), (192, 192, 256), 
 
 def config5_medium(shape, dx, rng, *, nonlinear: bool):
     """Water with seeded random ellipsoid inclusions (the config-4 recipe)."""
-    labels = ellipsoid_labels(shape, dx, 4, rng, semi_mm=(1.0, 4.0))
+    labels = ellipsoid_labels(shape, dx, 4, rng, semi_mm=(1.0, 4.0)).astype(np.uint8)
     beta_w = 3.5 if nonlinear else 0.0
     table = {0: (db_cm_to_np_m(0.0022), 1000.0, 1500.0, beta_w)}
     for j in range(1, 5):
@@ -266,15 +266,20 @@ def config5_medium(shape, dx, rng, *, nonlinear: bool):
     return Medium.from_labels(labels, table)
 
 
+_THERMAL_MEDIA: dict = {}
+
+
 def config5_thermal(shape, dx: float = 0.25e-3) -> dict:
     """The thermal phase a served request carries: soft tissue (k 0.5 W/m/K,
     rho 1000 kg/m^3, cp 3600 J/kg/K, perfusion 0.5/1050 1/s) on the request's
     grid, 0.05 s steps, 400 heating then 1200 cooling, CEM43 dose on."""
     from .thermal import ThermalMedium
 
-    return {"medium": ThermalMedium.homogeneous(tuple(shape), k=0.5, rho=1000.0, specific_heat=3600.0,
-                                                perfusion=0.5 / 1050.0, dx=dx),
-            "dt": 0.05, "n_heat": 400, "n_cool": 1200}
+    key = (tuple(shape), float(dx))
+    if key not in _THERMAL_MEDIA:  # homogeneous: one read-only instance per grid serves every request
+        _THERMAL_MEDIA[key] = ThermalMedium.homogeneous(tuple(shape), k=0.5, rho=1000.0, specific_heat=3600.0,
+                                                        perfusion=0.5 / 1050.0, dx=dx)
+    return {"medium": _THERMAL_MEDIA[key], "dt": 0.05, "n_heat": 400, "n_cool": 1200}
 
 
 def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear: float = 0.3,
@@ -300,7 +305,8 @@ def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear:
         nonlinear = bool(rng.random() < p_nonlinear)
         thermal = bool(rng.random() < p_thermal)
         grid = Grid(shape, dx, PMLSpec(pml * dx))
-        if rng.random() < p_reuse:
+        reused = bool(rng.random() < p_reuse)
+        if reused:
             key = (shape, nonlinear)
             if key not in pool:
                 pool[key] = config5_medium(shape, dx, np.random.default_rng((seed, len(pool))), nonlinear=nonlinear)
@@ -318,5 +324,6 @@ def config5_requests(n: int, seed: int = 5, *, grids=CONFIG5_GRIDS, p_nonlinear:
         frame = FieldFrame(dx=dx, grid_shape=shape, pml_vox=pml, apex_vox=apex, focus_vox=focus)
         reqs.append(Request(grid=grid, medium=med, source=src, spec=spec, nonlinear=nonlinear,
                             harmonics=(1, 2) if nonlinear else (1,), reference_point=focus, thermal=th, frame=frame,
-                            tag={"i": i, "shape": shape, "nonlinear": nonlinear, "thermal": thermal}))
+                            tag={"i": i, "shape": shape, "nonlinear": nonlinear, "thermal": thermal,
+                                 "reused": reused}))
     return reqs

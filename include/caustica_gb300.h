@@ -119,7 +119,9 @@ int cg_solver_info(const cg_solver* s, long long* out8);
  * counts, cg_solver_set_slabs, when CG_TUNE_SLABS=1) -- over
  * n_steps steps of the handle itself, keep the fastest and reset the
  * handle's state. The choice is remembered per (grid, batch, physics,
- * medium storage) for the process. out4 = {fused, persistent z, configurations
+ * medium storage) for the process; a batch of several members reuses the
+ * one-member choice of its grid when the process has one. out4 = {fused,
+ * persistent z, configurations
  * timed, 1 when taken from the process cache}. No counterpart in the
  * reference (it has one code path). */
 int cg_solver_autotune(cg_solver* s, int n_steps, int* out4);
@@ -307,6 +309,20 @@ int cg_heating_q(const cg_heating_spec* spec, float* q_dev, double* term_sums, v
  * to cg_pennes_set_coefficients / cg_pennes_set_labels as their q. */
 int cg_solver_heating_q(cg_solver* s, int member, const cg_heating_spec* spec, float* q_dev,
                         double* term_sums);
+
+/* Device-resident label volumes (a medium whose uint8 label map a caller
+ * keeps on the device and passes by pointer, as the Python fronts do for
+ * DLPack / __cuda_array_interface__ tensors): counts256[l] = voxels holding
+ * label l (the host picks the time step from the materials present,
+ * solvers/kspace/engine.py:86-113), and the labels at n flat voxel indices
+ * (the source scale 2 c dt / dx uses the local sound speed,
+ * engine.py:268-278). Both synchronise. */
+int cg_label_counts(const uint8_t* labels_dev, long long n, unsigned long long* counts256);
+int cg_gather_u8(const uint8_t* src_dev, const long long* idx, int n, uint8_t* out_host);
+/* cudaStreamSynchronize on a caller's stream (a producer stream named by
+ * __cuda_array_interface__ before its data is read on the library's own
+ * streams); NULL is the legacy default stream. */
+int cg_stream_synchronize(void* stream);
 
 /* Plain device buffers for callers without a CUDA runtime of their own. */
 int cg_buffer_alloc(size_t bytes, void** out);
