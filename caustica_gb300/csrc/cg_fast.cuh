@@ -254,11 +254,16 @@ constexpr int ct_odd(int n) { return (n % 2) ? n : n + 1; }
 // Exchange-buffer indexers. Row tiles: 16 pencils along threadIdx / 16, the
 // within-pencil index s along the lanes. Column tiles: pencils along the
 // lanes (threadIdx % 16).
-template <int A, int B>
+// WARP: every thread of the pencil sits in one warp (threads per pencil
+// divide 32 and pencils are consecutive in threadIdx), so the exchange of a
+// pencil's own slab needs only a warp barrier. Hazards between pencils
+// (staging buffers shared by a whole tile) keep their block barriers.
+template <int A, int B, bool WARP = false>
 struct RowEx {
   float2* base;  // this pencil's slab
   static constexpr int LD = ct_odd(B);
   static constexpr int SLAB = A * LD;
+  static constexpr bool kWarp = WARP;
   __device__ __forceinline__ float2& at(int k1, int n2) const { return base[k1 * LD + n2]; }
 };
 
@@ -266,8 +271,17 @@ template <int A, int B, int P = 16>
 struct ColEx {
   float2* base;  // + lane pencil
   static constexpr int SLAB = 0;
+  static constexpr bool kWarp = false;  // a column pencil spans the whole block
   __device__ __forceinline__ float2& at(int k1, int n2) const { return base[(k1 * B + n2) * P]; }
 };
+
+template <class Ex>
+__device__ __forceinline__ void ex_sync() {
+  if constexpr (Ex::kWarp)
+    __syncwarp();
+  else
+    __syncthreads();
+}
 
 // Twiddle table of an (A, B) transform in the order the threads read it:
 // twt[k1 * B + s] = exp(-2 pi i s k1 / N) (lanes run over s: conflict free).
@@ -300,12 +314,12 @@ __device__ __forceinline__ void fft2(const float2 (&v_in)[A], float2 (&w)[B], in
       ex.at(k1, s) = y;
     });
   }
-  __syncthreads();
+  ex_sync<Ex>();
   if (s < A) {
     static_for<0, B>([&](auto bi) { w[decltype(bi)::value] = ex.at(s, decltype(bi)::value); });
     Dft<B, INV>::run(w);
   }
-  __syncthreads();
+  ex_sync<Ex>();
 }
 
 // Asynchronous 16-byte global -> shared copy (L2 only), completed by

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(YT<N>::THREADS, YT<N>::MINB) kf_ypass(Dims d, 
                                                                         float2* __restrict__ S1,
                                                                         float2* __restrict__ S2) {
   constexpr int A = PSplit<N>::A, B = PSplit<N>::B, TPP = PSplit<N>::TPP;
-  using Ex = RowEx<A, B>;
+  using Ex = RowEx<A, B, (32 % TPP == 0)>;  // pencil-local exchange: warp barriers
   extern __shared__ float2 sm[];
   cgf::pdl_trigger();
   float2* tw = sm;  // (A, B) order

@@ -145,6 +145,9 @@ template <int N>
 __device__ __forceinline__ void z_split_store(float2* xb, const float2 (&X)[ZSplit<N>::A], float2* __restrict__ S,
                                               const Dims& d, int x, int y0, int p, int s, const float* mk) {
   constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B, NH = N / 2 + 1;
+  // every pencil of the tile is done with the buffer (its exchange slab or
+  // the staged spectrum) before any column lands in it
+  __syncthreads();
   if (s < B) static_for<0, A>([&](auto ai) {
     constexpr int a = decltype(ai)::value;
     xb[(s + B * a) * 17 + p] = X[a];
@@ -191,8 +194,8 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_u(Dims d, T
   cgf::fill_twt<B, A>(twf, t.twz);
   cgf::pdl_wait();
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
-  const RowEx<A, B> exi{sm + Z::OFF_EX + p * Z::EX};
-  const RowEx<B, A> exf{sm + Z::OFF_EX + p * Z::EX};
+  const RowEx<A, B, true> exi{sm + Z::OFF_EX + p * Z::EX};  // 16 threads per pencil: warp-local
+  const RowEx<B, A, true> exf{sm + Z::OFF_EX + p * Z::EX};
   const int ytiles = (d.ny + CG_ZROWS - 1) / CG_ZROWS;
   const int x = blockIdx.x / ytiles;
   const int y0 = (blockIdx.x - x * ytiles) * CG_ZROWS;
@@ -277,8 +280,8 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(Dims d, T
   cgf::pdl_wait();
   if (threadIdx.x == 0) s_peak = 0u;
   const int s = threadIdx.x & 15, p = threadIdx.x >> 4;
-  const RowEx<A, B> exi{sm + Z::OFF_EX + p * Z::EX};
-  const RowEx<B, A> exf{sm + Z::OFF_EX + p * Z::EX};
+  const RowEx<A, B, true> exi{sm + Z::OFF_EX + p * Z::EX};  // 16 threads per pencil: warp-local
+  const RowEx<B, A, true> exf{sm + Z::OFF_EX + p * Z::EX};
   const int ytiles = (d.ny + CG_ZROWS - 1) / CG_ZROWS;
   const int x = blockIdx.x / ytiles;
   const int y0 = (blockIdx.x - x * ytiles) * CG_ZROWS;
@@ -432,6 +435,7 @@ struct ZPShape {
   static constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B, NH = N / 2 + 1;
   static constexpr int TPP = ZSplit<N>::TPP;             // threads per pencil
   static constexpr int THREADS = CG_TILE * TPP;
+  static constexpr bool WARP = (32 % TPP) == 0;  // a pencil's threads in one warp
   static constexpr int MINB = TPP == 16 ? CG_FAST_MINB : 1;  // resident CTAs per SM
   // the field values of a thread load before its inverse transform unless
   // the transform's A values per thread leave no registers for them
@@ -606,8 +610,8 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       float2 v[A], w[B];
       z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, comp == 2 ? kz_s : nullptr);
       __syncthreads();  // the staging is read: the buffer becomes the exchange
-      const RowEx<A, B> exi{bufj + p * Z::EX};
-      const RowEx<B, A> exf{bufj + p * Z::EX};
+      const RowEx<A, B, Z::WARP> exi{bufj + p * Z::EX};
+      const RowEx<B, A, Z::WARP> exf{bufj + p * Z::EX};
       fft2<A, B, true>(v, w, s, sm, exi);
       if (!Z::EARLY) load_u();
       // u <- (u - dt/rho g) * absorb * sponge   (engine.py:462-464)
@@ -691,7 +695,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
         w[b] = make_float2(va ? __ldg(pb + rowa + n) : 0.f, va ? __ldg(pb + rowb + n) : 0.f);
       });
       float2* bufj = sm + Z::OFF_BUF + (size_t)jf * Z::BUF;
-      const RowEx<B, A> exf{bufj + p * Z::EX};
+      const RowEx<B, A, Z::WARP> exf{bufj + p * Z::EX};
       float2 X[A];
       fft2<B, A, false>(w, X, s, sm + N, exf);
       z_split_store<N>(bufj, X, S0 + b_idx * d.nspec, d, x, y0, p, s, nullptr);
@@ -742,8 +746,8 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     float2 v[A], w[B];
     z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, nullptr);
     __syncthreads();  // the staging is read: the buffer becomes the exchange
-    const RowEx<A, B> exi{bufj + p * Z::EX};
-    const RowEx<B, A> exf{bufj + p * Z::EX};
+    const RowEx<A, B, Z::WARP> exi{bufj + p * Z::EX};
+    const RowEx<B, A, Z::WARP> exf{bufj + p * Z::EX};
     fft2<A, B, true>(v, w, s, sm, exi);
     if (!Z::EARLY) load_p();
     const float spx = t.sx[x];
