@@ -656,7 +656,6 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   using Z = ZPShape<N>;
   constexpr int A = Z::A, B = Z::B;
   extern __shared__ float2 sm[];
-  __shared__ unsigned int s_peak;
   const int ytiles = (d.ny + CG_ZROWS - 1) / CG_ZROWS;  // ny even; the last tile may be ragged
   const long long per_member = (long long)d.nx * ytiles;
   const long long total = per_member * n_members;
@@ -666,7 +665,6 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   if (t0 >= t1) return;  // the whole CTA, before any barrier
   zp_tables<N, false>(sm, t, m);
   cgf::pdl_wait();
-  if (threadIdx.x == 0) s_peak = 0u;
   const float* sz_s = Z::TBL ? reinterpret_cast<const float*>(sm + Z::OFF_SZ) : t.sz;
   const float4* tab_s = reinterpret_cast<const float4*>(sm + Z::OFF_TAB);
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
@@ -705,6 +703,9 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   prefetch(t0, 0);
   const long long n_step = ctl[0] + n_local;
   const int m_bin = (int)(n_step % rec.spp);
+  const long long per_log = n_step / rec.spp;
+  unsigned int wpeak = 0u;
+  long long wmember = -1;
   const long long Ry = rec.hi[1] - rec.lo[1], Rz = rec.hi[2] - rec.lo[2];
   const bool drive_on = src.S > 0 && n_step < src.n_drive;
   const float4 dr = drive_on ? src.drive[n_step] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -855,20 +856,23 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
         });
       }
     }
+    // convergence peak: a running max per warp over its tiles, written to
+    // the period log (an integer max over the float bits) when the batch
+    // member changes and at the end -- no barrier per tile
     lpeak = __reduce_max_sync(0xffffffffu, lpeak);
-    if ((threadIdx.x & 31) == 0 && lpeak) atomicMax(&s_peak, lpeak);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      if (s_peak != 0u) {
-        const long long per = n_step / rec.spp;
-        if (per < rec.max_periods) atomicMax(&rec.peaks[b_idx * rec.max_periods + per], s_peak);
-      }
-      s_peak = 0u;  // the next tile's updates follow the next item's barrier
+    if (b_idx != wmember) {
+      if ((threadIdx.x & 31) == 0 && wpeak && per_log < rec.max_periods)
+        atomicMax(&rec.peaks[wmember * rec.max_periods + per_log], wpeak);
+      wpeak = 0u;
+      wmember = b_idx;
     }
+    wpeak = max(wpeak, lpeak);
     float2 X[A];
     fft2<B, A, false>(w, X, s, sm + N, exf);
     z_split_store<N>(bufj, X, S, d, x, y0, p, s, nullptr);
   }
+  if ((threadIdx.x & 31) == 0 && wpeak && wmember >= 0 && per_log < rec.max_periods)
+    atomicMax(&rec.peaks[wmember * rec.max_periods + per_log], wpeak);
 }
 
 // ------------------------------------------------ per-length launchers --
