@@ -113,7 +113,21 @@ class Medium:
             for i in present:
                 lut[int(i)] = np.asarray(table[int(i)], np.float32)
             out = [np.ascontiguousarray(lut[:, k])[id_map] for k in range(4)]
-            return cls(*out, id_map=id_map)
+            med = cls(*out, id_map=id_map)
+            lo, hi = int(present[0]), int(present[-1])
+            if hi - lo < 256:
+                # the label decomposition the solver needs, known by construction:
+                # labels id - lo and one row per id (absent ids repeat the first
+                # present row), kept with read-only maps so it stays true
+                rows = lut[lo:hi + 1].copy()
+                absent = np.setdiff1d(np.arange(lo, hi + 1), present) - lo
+                rows[absent] = rows[0]
+                labels = (id_map - lo).astype(np.uint8) if lo else id_map.astype(np.uint8)
+                maps = (med.alpha, med.rho, med.c, med.beta)
+                for m in (*maps, labels, rows):
+                    m.setflags(write=False)
+                med._label_cache = (maps, labels, rows)
+            return med
         out = [np.zeros(id_map.shape, np.float32) for _ in range(4)]
         for i in present:
             mask = id_map == i

@@ -278,8 +278,18 @@ def label_volumes(vols, id_map=None, max_labels: int = 256):
 
 
 def label_medium(medium, max_labels: int = 256):
-    """Labels of the acoustic property volumes (alpha, rho, c, beta), or None."""
+    """Labels of the acoustic property volumes (alpha, rho, c, beta), or None.
+
+    A medium built by ``Medium.from_labels`` carries its decomposition with
+    read-only maps; it is used as it is while the medium still holds those
+    very arrays (nothing can have changed them). Any other medium is
+    decomposed and verified against its maps."""
     vols = [getattr(medium, k) for k in ("alpha", "rho", "c", "beta")]
+    cached = getattr(medium, "_label_cache", None)
+    if cached is not None:
+        maps, labels, rows = cached
+        if all(v is m for v, m in zip(vols, maps)) and not any(m.flags.writeable for m in maps):
+            return labels, rows
     return label_volumes(vols, getattr(medium, "id_map", None), max_labels)
 
 

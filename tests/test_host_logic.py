@@ -178,3 +178,24 @@ def test_label_decomposition_without_an_id_map_is_exact_for_rare_materials(n_mat
     lab, props = eng.label_volumes(vols)
     for j in range(4):
         np.testing.assert_array_equal(props[lab, j].view(np.uint32), vols[j].view(np.uint32))
+
+
+def test_label_built_media_carry_their_decomposition_and_lose_it_when_a_map_changes():
+    from caustica_gb300.engine import label_medium, label_volumes
+
+    rng = np.random.default_rng(12)
+    ids = rng.integers(3, 7, (10, 12, 14)).astype(np.int32)  # ids 3..6, lo = 3
+    ids[ids == 5] = 6  # id 5 absent inside the range
+    table = {i: (0.5 * i, 900.0 + i, 1450.0 + 10 * i, 0.0) for i in range(3, 7)}
+    med = ct.Medium.from_labels(ids, table)
+    vols = [med.alpha, med.rho, med.c, med.beta]
+    want = label_volumes(vols, med.id_map)
+    got = label_medium(med)
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[1], want[1])
+    assert not med.c.flags.writeable  # the decomposition stays true
+    # replacing a map drops the shortcut: the new maps are decomposed and verified
+    med.c = med.c.copy()
+    med.c[0, 0, 0] = 1999.0
+    lab, props = label_medium(med)
+    np.testing.assert_array_equal(props[lab][..., 2], med.c)
