@@ -297,7 +297,7 @@ class Server:
     """Continuous-batching CW solve server on one GPU."""
 
     def __init__(self, hbm_budget_bytes: int | None = None, max_pack: int = 8, poll_s: float = 2e-4,
-                 thermal_workers: int = 3, max_active: int = 6, plan_workers: int = 4):
+                 thermal_workers: int = 3, max_active: int = 6, plan_workers: int = 4, device: int = 0):
         if hbm_budget_bytes is None:
             hbm_budget_bytes = 200 << 30
         self.budget = int(hbm_budget_bytes)
@@ -309,7 +309,10 @@ class Server:
         # small pool as soon as it is submitted, off the scheduler thread
         from concurrent.futures import ThreadPoolExecutor
 
-        self._planner = ThreadPoolExecutor(max(1, int(plan_workers)), thread_name_prefix="cg-plan")
+        # every thread of the server works on `device` (the CUDA device is per thread)
+        self.device = int(device)
+        self._planner = ThreadPoolExecutor(max(1, int(plan_workers)), thread_name_prefix="cg-plan",
+                                           initializer=self._bind_device)
         self._planning: dict = {}
         self._plans_lock = threading.Lock()
         self.poll_s = float(poll_s)
@@ -460,7 +463,13 @@ class Server:
             else:
                 fut.set_result(oc)
 
+    def _bind_device(self) -> None:
+        from . import _lib
+
+        _lib.call("cg_set_device", self.device)
+
     def _loop(self) -> None:
+        self._bind_device()
         while True:
             with self._lock:
                 if self._stop and not self._pending and not self._active:
@@ -490,6 +499,7 @@ class Server:
                 time.sleep(self.poll_s)
 
     def _thermal_loop(self) -> None:
+        self._bind_device()
         while True:
             item = self._thermal_q.get()
             if item is None:
