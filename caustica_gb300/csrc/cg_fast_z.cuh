@@ -561,24 +561,28 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   const bool lab = m.labels != nullptr;
   const int s = threadIdx.x % Z::TPP, p = threadIdx.x / Z::TPP;
   auto spec = [&](int comp, long long b) { return (comp == 0 ? S1 : (comp == 1 ? S0 : S2)) + b * d.nspec; };
+  // tiles run member-fastest: the members of one (x, y0) follow each other,
+  // so the tile's labels load once for all of them (label slot per group)
+  auto label_slot = [&](long long tile) { return (int)((tile / n_members - t0 / n_members) & 1); };
   auto prefetch = [&](long long tile, int comp, int j) {
-    const long long b = tile / per_member, r = tile - b * per_member;
+    const long long b = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), spec(comp, b), d, x, y0);
-    if (comp == 0 && lab) z_prefetch_labels<N>(lab0 + ((tile - t0) & 1) * CG_ZROWS * N, m.labels, d, x, y0);
+    if (comp == 0 && lab && (tile == t0 || b == 0))
+      z_prefetch_labels<N>(lab0 + label_slot(tile) * CG_ZROWS * N, m.labels, d, x, y0);
     cgf::cp_async_commit();
   };
   prefetch(t0, 0, 0);
   int j = 0;
   for (long long tile = t0; tile < t1; ++tile) {
-    const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
+    const long long b_idx = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     const int ya = y0 + 2 * p, yb = ya + 1;
     const bool va = ya < d.ny;  // this pencil's rows exist (ny even: yb too)
     const float spx = t.sx[x];
     const float spa = va ? spx * t.sy[ya] : 0.f, spb = va ? spx * t.sy[yb] : 0.f;
     const long long rowa = ((long long)x * d.ny + ya) * N, rowb = rowa + N;
-    const uint8_t* la = lab0 + ((tile - t0) & 1) * CG_ZROWS * N + (2 * p) * N;
+    const uint8_t* la = lab0 + label_slot(tile) * CG_ZROWS * N + (2 * p) * N;
     const uint8_t* lb = la + N;
 #pragma unroll 1
     for (int comp = 0; comp < 3; ++comp, j ^= 1) {
@@ -670,17 +674,20 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   uint8_t* lab0 = reinterpret_cast<uint8_t*>(sm + Z::OFF_LAB);
   const bool lab = m.labels != nullptr;
   const int s = threadIdx.x % Z::TPP, p = threadIdx.x / Z::TPP;
+  // tiles run member-fastest: the members of one (x, y0) follow each other,
+  // so the tile's labels load once for all of them (label slot per group)
+  auto label_slot = [&](long long tile) { return (int)((tile / n_members - t0 / n_members) & 1); };
   auto prefetch = [&](long long tile, int j) {
-    const long long b = tile / per_member, r = tile - b * per_member;
+    const long long b = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), S0 + b * d.nspec, d, x, y0);
-    if (lab) z_prefetch_labels<N>(lab0 + j * CG_ZROWS * N, m.labels, d, x, y0);
+    if (lab && (tile == t0 || b == 0)) z_prefetch_labels<N>(lab0 + label_slot(tile) * CG_ZROWS * N, m.labels, d, x, y0);
     cgf::cp_async_commit();
   };
   if constexpr (FWD) {
     int jf = 0;
     for (long long tile = t0; tile < t1; ++tile, jf ^= 1) {
-      const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
+      const long long b_idx = tile % n_members, r = tile / n_members;
       const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
       const int ya = y0 + 2 * p;
       const bool va = ya < d.ny;  // ny even: row ya + 1 too
@@ -719,7 +726,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   });
   int j = 0;
   for (long long tile = t0; tile < t1; ++tile, j ^= 1) {
-    const long long b_idx = tile / per_member, r = tile - b_idx * per_member;
+    const long long b_idx = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     const int ya = y0 + 2 * p, yb = ya + 1;
     const bool va = ya < d.ny;  // this pencil's rows exist (ny even: yb too)
@@ -742,7 +749,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     __syncthreads();
     if (tile + 1 < t1) prefetch(tile + 1, j ^ 1);
     float2* bufj = sm + Z::OFF_BUF + (size_t)j * Z::BUF;
-    const uint8_t* la = lab0 + j * CG_ZROWS * N + (2 * p) * N;
+    const uint8_t* la = lab0 + label_slot(tile) * CG_ZROWS * N + (2 * p) * N;
     const uint8_t* lb = la + N;
     float2 v[A], w[B];
     z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, nullptr);
