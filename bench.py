@@ -380,6 +380,8 @@ def run_gb300(args, dist, rank, ws, local):
                        "step": f"one full solve ({res.steps_total} time steps, {res.steps_total // plan.spp} periods) "
                                f"through WesterveltKSpaceGB300.run() from host numpy",
                        "seconds": el, "solves_per_s": ws / el}
+    if rank == 0 and ws == 1 and not args.skip_e2e and not args.skip_store:
+        line["store"] = bench_store(grid, med, src, spec, job)
     if rank == 0 and ws == 1 and not args.skip_batched:
         line["batched"] = bench_batched()
     if rank == 0 and ws == 1 and not args.skip_serving:
@@ -395,6 +397,41 @@ def run_gb300(args, dist, rank, ws, local):
     line["clocks"] = clk.summary()
     if rank == 0:
         print(json.dumps(line, default=_jsonable), flush=True)
+
+
+def bench_store(grid, med, src, spec, job):
+    """Store quantisation of one config-2 result (harmonics 1-3 and p_max:
+    seven float32 fields of the record region): the device path inside a
+    solve (``store_quantize``: two passes over each field on the GPU, then
+    only the float16 bytes to the host) against the reference's host
+    ``try_float16`` on the same fields (io/quantize.py:45-67, NumPy, one
+    core), which its ``save_result`` runs before writing."""
+    from caustica_gb300 import store
+    from caustica_gb300.solvers import WesterveltKSpaceGB300
+    from oracle import quantize as oq
+
+    solver = WesterveltKSpaceGB300()
+    solver.store_quantize = store.DEFAULT_MAX_NORM_ERR
+    t0 = time.perf_counter()
+    res = solver.run(grid, med, src, spec, harmonics=job["harmonics"], reference_point=job["reference_point"])
+    solve_s = time.perf_counter() - t0
+    att = res.meta["quantized"]
+    fields = oq.store_order(res.phasors, res.p_max)
+    t1 = time.perf_counter()
+    host = [oq.try_float16(f) for _, f in fields]
+    host_s = time.perf_counter() - t1
+    same = all(np.array_equal(np.asarray(att["fields"][n].stored).view(np.uint8), np.asarray(h.stored).view(np.uint8))
+               and att["fields"][n].scale == h.scale for (n, _), h in zip(fields, host))
+    return {"workload": f"{len(fields)} float32 fields of {res.p_max.size} voxels (p_real/p_imag of harmonics "
+                        f"{sorted(res.phasors)} and p_max, config 2)",
+            "device_s": att["seconds"], "stored_bytes": int(sum(q.stored.nbytes for q in att["fields"].values())),
+            "float32_bytes": int(sum(f.nbytes for _, f in fields)),
+            "dtypes": sorted({q.dtype_name for q in att["fields"].values()}),
+            "solve_with_store_s": solve_s, "equal_to_host": bool(same),
+            "cpu_baseline": {"value": host_s, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "try_float16 of the same fields (NumPy)"},
+            "timing": "device: wall clock of cg_solver_quantize (both passes, the float16 copy to fresh host "
+                      "pages) inside the solve; host: wall clock of the NumPy restatement"}
 
 
 def bench_batched(n_plain: int = 4):
@@ -571,6 +608,7 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--skip-thermal", action="store_true")
+    ap.add_argument("--skip-store", action="store_true")
     ap.add_argument("--prerun-periods", type=int, default=None,
                     help="periods run before the warm-up (default: the settle floor of the workload)")
     args = ap.parse_args()

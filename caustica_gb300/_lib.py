@@ -55,6 +55,10 @@ class PennesConfig(C.Structure):
     ]
 
 
+class QField(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("n", C.c_longlong), ("stride", C.c_longlong)]
+
+
 class FocusInput(C.Structure):
     _fields_ = [
         ("p1", C.c_void_p), ("p2", C.c_void_p), ("pmax", C.c_void_p),
@@ -133,6 +137,8 @@ SIGNATURES = {
     "cg_solver_focus_metrics": [_P, _I, C.POINTER(FocusInput), C.POINTER(FocusReport)],
     "cg_heating_q": [C.POINTER(HeatingSpec), _P, _P, _P],
     "cg_solver_heating_q": [_P, _I, C.POINTER(HeatingSpec), _P, _P],
+    "cg_quantize_f16": [C.POINTER(QField), _I, C.c_double, _P, _P, _P, _P],
+    "cg_solver_quantize": [_P, _I, C.c_double, _P, _P, _P],
     "cg_label_counts": [_P, _LL, _P],
     "cg_gather_u8": [_P, _P, _I, _P],
     "cg_stream_synchronize": [_P],

@@ -20,10 +20,11 @@ from .engine import DeviceSolver, make_plan, solve
 def solve_steering(grid, medium, indices, phases, *, f0: float, amplitude: float, spec: CWRunSpec | None = None,
                    nonlinear: bool = False, harmonics=(1,), record_region=None, reference_point=None,
                    ramp_periods: float = 3.0, max_batch: int | None = None, name: str = "steering_gb300",
-                   result_cls=SolverResult) -> list:
+                   result_cls=SolverResult, quantize: float | None = None) -> list:
     """Solve B steering positions; ``phases`` is (B, n_voxels) float32, host
     or device (a device array is read back: the source scale is formed with
-    the host's float32 arithmetic either way)."""
+    the host's float32 arithmetic either way). ``quantize`` also attaches
+    each member's device-quantised store fields (``meta["quantized"]``)."""
     from .device import is_device_array, to_host
 
     if is_device_array(phases):
@@ -42,5 +43,5 @@ def solve_steering(grid, medium, indices, phases, *, f0: float, amplitude: float
     for lo in range(0, B, chunk):
         part = phases[lo:lo + chunk]
         with DeviceSolver(plan, batch=part.shape[0], phases=part) as dev:
-            out.extend(solve(plan, phases=part, dev=dev, result_cls=result_cls))
+            out.extend(solve(plan, phases=part, dev=dev, result_cls=result_cls, quantize=quantize))
     return out

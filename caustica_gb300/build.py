@@ -25,7 +25,7 @@ LIB = PKG / "libcaustica_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # the size-specialised passes are split into several units per family (one
 # length group each) so the parallel build finishes in about a minute
-SOURCES = (["cg_kspace.cu", "cg_pennes.cu", "cg_post.cu", "cg_fused_xy.cu", "cg_fast_yx.cu", "cg_fast_z.cu"]
+SOURCES = (["cg_kspace.cu", "cg_pennes.cu", "cg_post.cu", "cg_store.cu", "cg_fused_xy.cu", "cg_fast_yx.cu", "cg_fast_z.cu"]
            + [f"cg_fast_yx_{g}.cu" for g in "abcdef"] + [f"cg_fast_z_{g}.cu" for g in "abcdef"])
 
 

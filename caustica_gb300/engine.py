@@ -805,7 +805,7 @@ def member_schedule(peaks: np.ndarray, plan: Plan, name: str | None = None):
 
 
 def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result_cls=SolverResult,
-          dev: DeviceSolver | None = None):
+          dev: DeviceSolver | None = None, quantize: float | None = None):
     """Run the settle + record schedule; one result per batch member.
 
     With ``phases`` of shape (B, S) the B members share the medium and the
@@ -814,6 +814,10 @@ def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result
     are replayed from its period peaks, and a member whose stand-alone run
     would have stopped settling at a different period is solved again on
     its own, so each result equals the one its solo run gives.
+
+    ``quantize`` (a bound on the relative round-trip error) also quantises
+    each member's stored fields on the device for the result store and
+    attaches them as ``meta["quantized"]``.
     """
     t0 = time.monotonic()
     batch = 1 if phases is None else int(np.atleast_2d(phases).shape[0])
@@ -861,11 +865,18 @@ def solve(plan: Plan, *, progress=None, phases: np.ndarray | None = None, result
                                 "medium_storage": "dense" if plan.dense is not None else "labels",
                                 "batch": batch, "member": b})
             results.append(_results(plan, dev, ph, pm, common, b, result_cls))
+            if quantize is not None:
+                from .store import quantize_solver
+
+                tq = time.perf_counter()
+                fields = quantize_solver(dev, b, quantize)
+                results[-1].meta["quantized"] = {"max_norm_err": float(quantize), "fields": fields,
+                                                 "seconds": time.perf_counter() - tq}
     finally:
         if own:
             dev.close()
     for b in redo:
-        solo = solve(plan, phases=np.atleast_2d(phases)[b:b + 1], result_cls=result_cls)[0]
+        solo = solve(plan, phases=np.atleast_2d(phases)[b:b + 1], result_cls=result_cls, quantize=quantize)[0]
         solo.meta.update({"batch": batch, "member": b, "solved_alone": True})
         results[b] = solo
     return results

@@ -60,6 +60,7 @@ class LinearKSpaceGB300(SolverBase):
         front = self._front()
         front.caps = self.caps
         front.validate = self.validate  # caustica's own SolverBase.validate
+        front.store_quantize = getattr(self, "store_quantize", None)
         return _run(front, (grid, medium, source, spec), kwargs)
 
 
@@ -76,6 +77,7 @@ class WesterveltKSpaceGB300(SolverBase):
         front = self._front()
         front.caps = self.caps
         front.validate = self.validate
+        front.store_quantize = getattr(self, "store_quantize", None)
         return _run(front, (grid, medium, source, spec), kwargs)
 
 

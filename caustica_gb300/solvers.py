@@ -32,6 +32,10 @@ class KSpaceGB300Base:
     result_cls = contract.SolverResult
     spec_cls = contract.CWRunSpec
     capability_error = contract.SolverCapabilityError
+    # a bound on the relative round-trip error (1e-3 is the store's default):
+    # run() then also quantises the stored fields on the device, for
+    # caustica_gb300.store.save_result, as result.meta["quantized"]
+    store_quantize: float | None = None
 
     def validate(self, grid, medium, source) -> None:
         contract.validate_setup(self.name, self.caps, grid, medium, source)
@@ -47,7 +51,7 @@ class KSpaceGB300Base:
         if checkpoint is not None:
             return run_with_checkpoint(plan, checkpoint, progress=progress, result_cls=self.result_cls,
                                        grid=grid, medium=medium, source=source)
-        return solve(plan, progress=progress, result_cls=self.result_cls)[0]
+        return solve(plan, progress=progress, result_cls=self.result_cls, quantize=self.store_quantize)[0]
 
 
 class LinearKSpaceGB300(KSpaceGB300Base):

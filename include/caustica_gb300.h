@@ -310,6 +310,40 @@ int cg_heating_q(const cg_heating_spec* spec, float* q_dev, double* term_sums, v
 int cg_solver_heating_q(cg_solver* s, int member, const cg_heating_spec* spec, float* q_dev,
                         double* term_sums);
 
+/* Dynamic float16 quantisation of stored result fields: the output
+ * contract of the caustica-result/1 store (try_float16, io/quantize.py:45-67,
+ * called per field by _quantized_dataset, io/store.py:69-89). Per field
+ * (n float32 values, `stride` floats apart: 1 for p_max, 2 for the real or
+ * imaginary part of a complex64 phasor): peak = max |x|; a zero peak stores
+ * the plain float16 cast with scale 1; otherwise q = half_rn(x / peak) and
+ * err = max |float(q) * peak - x| / peak, all float32 operations as NumPy
+ * performs them, and the field keeps float16 with scale = peak when
+ * err <= max_norm_err, else its float32 values with scale 1 (a NaN peak
+ * always falls back, like the reference's NaN error). Outputs, per field f
+ * at the offset of its first value in the concatenation of all fields:
+ * f16_out gets the float16 bits of float16 fields, f32_out the values of
+ * float32 fields (may be NULL when none falls back; the call then fails if
+ * one does); info[4 f + 0..3] = scale, norm_err, 1 for float16 / 0 for
+ * float32, and the peak. Outputs may be host or device memory; the fields
+ * must be device memory. Synchronises before return. */
+#define CG_QUANT_MAX_FIELDS 32
+typedef struct cg_qfield {
+  const float* data;
+  long long n;
+  long long stride;
+} cg_qfield;
+
+int cg_quantize_f16(const cg_qfield* fields, int n_fields, double max_norm_err, uint16_t* f16_out,
+                    float* f32_out, float* info, void* stream);
+/* The same on member `member`'s result of the last cg_solver_finalize, in
+ * the order the store writes its datasets: for each recorded harmonic in
+ * ascending order p_real_h{n} then p_imag_h{n}, then p_max; each field has
+ * the record region's voxel count (io/store.py:146-151). Finalize may be
+ * called with NULL outputs first, so the float32 result never crosses to
+ * the host. */
+int cg_solver_quantize(cg_solver* s, int member, double max_norm_err, uint16_t* f16_out, float* f32_out,
+                       float* info);
+
 /* Device-resident label volumes (a medium whose uint8 label map a caller
  * keeps on the device and passes by pointer, as the Python fronts do for
  * DLPack / __cuda_array_interface__ tensors): counts256[l] = voxels holding
