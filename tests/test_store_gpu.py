@@ -138,3 +138,19 @@ def test_save_result_from_a_solve_writes_the_device_fields(tmp_path, monkeypatch
     g = h5stub.tree(path2)
     for name, _ in oq.store_order(res.phasors, res.p_max):
         assert np.array_equal(bits(g[f"output/{name}"].data), bits(f[f"output/{name}"].data))
+
+
+@pytest.mark.parametrize("shape", [(96,), (40, 36)])
+def test_one_and_two_dimensional_results(shape):
+    dx = C0 / (F0 * 6.0)
+    grid = cg.Grid(shape, dx, cg.PMLSpec(8 * dx))
+    med = cg.Medium.homogeneous(grid.shape, alpha_np_m=0.0253, rho=1000.0, c=C0, beta=3.5)
+    idx = np.array([[12] + [n // 2 for n in shape[1:]]])
+    src = cg.CWSource(indices=idx, phases=np.zeros(1, np.float32), amplitude=1e5, f0=F0)
+    solver = cg.WesterveltKSpaceGB300()
+    solver.store_quantize = 5e-4
+    res = solver.run(grid, med, src, cg.CWRunSpec(min_settle_periods=2, max_settle_periods=4), harmonics=(1, 2))
+    for name, f in oq.store_order(res.phasors, res.p_max):
+        q = res.meta["quantized"]["fields"][name]
+        same(q, oq.try_float16(f, 5e-4))
+        assert q.stored.shape == res.p_max.shape
