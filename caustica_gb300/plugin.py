@@ -122,3 +122,25 @@ def install_compat() -> None:
         planner.estimate = estimate
         if hasattr(runner, "estimate"):
             runner.estimate = estimate
+
+
+def result_store(root, *, probe: bool = True):
+    """caustica's own ``ResultStore`` (io/store.py:338-398) whose ``save`` quantises on the GPU.
+
+    The directory plumbing -- verified mkdir, write probe, temp-debris sweep,
+    the resume scan, ``load`` -- is the reference's; ``save`` writes the same
+    ``caustica-result/1`` file through :func:`caustica_gb300.store.save_result`,
+    so the float16 fields a GB300 solve attached (or the result's arrays,
+    quantised on the device) are stored without a host quantisation pass.
+    caustica's store module imports h5py, so this needs it as well.
+    """
+    from caustica.io import store as ref_store
+
+    from . import store as gb_store
+
+    class ResultStoreGB300(ref_store.ResultStore):
+        def save(self, name, result, source, **kwargs):
+            ref_store.ensure_dir_verified(self.root)  # re-verified at write time, as the reference's save does
+            return gb_store.save_result(self.path(name), result, source, **kwargs)
+
+    return ResultStoreGB300(root, probe=probe)

@@ -60,6 +60,9 @@ class Request:
     # {"medium", "dt", "n_heat", "n_cool", "T0", "q_scale", "harmonics", "alpha_power_law_y"}
     thermal: dict | None = None
     frame: Any = None  # a metrics.FieldFrame: focal metrics are computed when given
+    # a bound on the relative round-trip error: the result store's float16
+    # fields are quantised on the device as well (result.meta["quantized"])
+    store_quantize: float | None = None
     tag: Any = None
 
 
@@ -244,7 +247,7 @@ def _result_cls():
 
 
 def _post_process(dev, member: int, result, req: Request):
-    """Focal metrics and heating Q of one member from the handle's device phasors."""
+    """Focal metrics, heating Q and store fields of one member from the handle's device phasors."""
     from .metrics import device_focus_metrics
     from .sensors import HeatingSource
 
@@ -252,6 +255,11 @@ def _post_process(dev, member: int, result, req: Request):
     if req.frame is not None:
         metrics = device_focus_metrics(dev, member, result, req.frame, source_amplitude=float(req.source.amplitude),
                                        medium=req.medium)
+    if req.store_quantize is not None:
+        from .store import quantize_solver
+
+        result.meta["quantized"] = {"max_norm_err": float(req.store_quantize),
+                                    "fields": quantize_solver(dev, member, req.store_quantize)}
     heating = None
     if req.thermal is not None:
         th = req.thermal

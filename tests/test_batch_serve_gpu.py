@@ -174,3 +174,26 @@ def test_requests_arriving_while_the_gpu_is_busy_pack_across_arrivals():
     for r, o in zip(late, outs[1:]):
         solo = _solo(r.grid, r.medium, r.source.indices, r.source.phases, r.spec, False)
         assert rel_l2(o.result.phasor, solo.phasor) < 1e-6, r.tag
+
+
+def test_served_requests_carry_device_store_fields_of_their_own_result():
+    from oracle import quantize as oq
+
+    spec = cg.CWRunSpec(convergence_tol=0.0, min_settle_periods=2, max_settle_periods=2, n_record_periods=1)
+    grid, med, idx, rng = _setup((16, 16, 24), 41, nonlinear=True)
+    reqs = [serve.Request(grid=grid, medium=med, nonlinear=True, harmonics=(1, 2), spec=spec, store_quantize=1e-3,
+                          source=cg.CWSource(indices=idx, phases=rng.uniform(-3, 3, len(idx)).astype(np.float32),
+                                             amplitude=2e5, f0=1e6))
+            for _ in range(3)]
+    reqs.append(serve.Request(grid=grid, medium=med, nonlinear=True, harmonics=(1, 2), spec=spec,
+                              source=reqs[0].source))
+    with serve.Server() as srv:
+        outs = [f.result(timeout=300) for f in [srv.submit(r) for r in reqs]]
+    for o in outs[:3]:
+        q = o.result.meta["quantized"]
+        for name, f in oq.store_order(o.result.phasors, o.result.p_max):
+            ref = oq.try_float16(f)
+            got = q["fields"][name]
+            assert got.dtype_name == ref.dtype_name and got.scale == ref.scale and got.norm_err == ref.norm_err
+            assert np.array_equal(np.asarray(got.stored).view(np.uint8), np.asarray(ref.stored).view(np.uint8))
+    assert "quantized" not in outs[3].result.meta

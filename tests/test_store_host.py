@@ -233,3 +233,20 @@ def test_restore_is_the_reload_recipe():
     q = oq.try_float16(np.array([1.0, -3.5, 0.25], np.float32))
     assert np.array_equal(store.restore(q.stored, q.scale), oq.restore(q.stored, q.scale))
     assert store.Quantized(*q).restore().dtype == np.float32
+
+
+@pytest.mark.skipif(REF is None, reason="reference sources not present")
+def test_the_reference_result_store_saves_through_the_gb300_writer(tmp_path, monkeypatch):
+    h5stub.install(monkeypatch)
+    monkeypatch.syspath_prepend(str(REF))
+    for mod in [m for m in sys.modules if m == "caustica" or m.startswith("caustica.") or m == "caustica_gb300.plugin"]:
+        monkeypatch.delitem(sys.modules, mod)
+    plugin = importlib.import_module("caustica_gb300.plugin")
+    rs = plugin.result_store(tmp_path / "results")
+    res = _result()
+    q = _oracle_fields(res)
+    path = rs.save("cfg2_a", res, _source(), dx=1.5e-4, grid_shape=(192, 192, 256), quantized=q)
+    assert path == rs.path("cfg2_a") and rs.is_complete("cfg2_a")
+    assert rs.completed() == ["cfg2_a"] and rs.missing(["cfg2_a", "cfg2_b"]) == ["cfg2_b"]
+    back = rs.load("cfg2_a")
+    assert np.array_equal(back.p_max, oq.restore(q["p_max"].stored, q["p_max"].scale))
