@@ -167,18 +167,20 @@ FAST_SIZES = {8, 16, 24, 32, 48, 64, 96, 128, 160, 192, 256}  # every size-speci
 FAST_XYZ_SIZES = FAST_SIZES | {320, 400, 512, 640}  # x/y passes and the persistent z-passes only
 
 
-def slot_symbols(padded3, persistent_z: bool = True) -> list[str]:
+def slot_symbols(padded3, persistent_z: bool = True, tma: bool = False) -> list[str]:
     """The kernel each step slot launches on this grid (size-specialised where the axis allows);
-    ``persistent_z`` is the autotuner's z-pass choice (lengths without a per-tile kernel are always
-    persistent when ny is even)."""
+    ``persistent_z`` and ``tma`` are the autotuner's z-pass choices (lengths without a per-tile
+    kernel are always persistent when ny is even; ``tma``: tensor-map staging of the z-tiles)."""
     nx, ny, nz = padded3
     y = f"kf_ypass<{ny},{{}}>" if ny in FAST_XYZ_SIZES else "k_ypass"
     x = f"kf_xpass<{nx},{{}}>" if nx in FAST_XYZ_SIZES else "k_xpass"
     zp = "kfp" if ny % 2 == 0 and (persistent_z or nz not in FAST_SIZES) else "kf"
     zfast = nz in (FAST_XYZ_SIZES if zp == "kfp" else FAST_SIZES)
-    zu = f"{zp}_zpass_u<{nz}>" if zfast else "k_zpass_u"
+    tma = bool(tma and zp == "kfp" and zfast)
+    zu = (f"{zp}_zpass_u<{nz},true>" if tma else f"{zp}_zpass_u<{nz}>") if zfast else "k_zpass_u"
     # the timed steps do not record: the persistent p-pass runs its record-free instantiation
-    zpp = (f"{zp}_zpass_p<{nz},false>" if zp == "kfp" else f"kf_zpass_p<{nz},1>") if zfast else "k_zpass_p"
+    zpp = ((f"{zp}_zpass_p<{nz},false,false,true>" if tma else f"{zp}_zpass_p<{nz},false>") if zp == "kfp"
+           else f"kf_zpass_p<{nz},1>") if zfast else "k_zpass_p"
     return [y.format("Y_FWD"), x.format("X_GRAD"), y.format("Y_INV_GRAD"), zu, y.format("Y_FWD_DIV"),
             x.format("X_DIV"), y.format("Y_INV"), zpp]
 
@@ -331,7 +333,8 @@ def run_gb300(args, dist, rank, ws, local):
     dom = int(np.argmax(per_launch_ms))
     achieved = bytes_slot[dom] / (per_launch_ms[dom] * 1e-3) / 1e9
     kernel_name = SLOTS[dom]
-    symbols = slot_symbols(plan.padded3, bool((tuning or {}).get("persistent_z", True)))
+    symbols = slot_symbols(plan.padded3, bool((tuning or {}).get("persistent_z", True)),
+                           bool((tuning or {}).get("tma_staging", False)))
     traffic = _traffic_from_profiles(kernel_name)
     step_b = step_algorithmic_bytes(info_labels, True)
     step_achieved = step_b * value / ws / 1e9

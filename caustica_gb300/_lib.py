@@ -116,6 +116,8 @@ SIGNATURES = {
     "cg_solver_profile": [_P, _I, _I, _P],
     "cg_solver_autotune": [_P, _I, _P],
     "cg_solver_set_slabs": [_P, _I],
+    "cg_solver_set_zstaging": [_P, _I],
+    "cg_solver_get_zstaging": [_P, _P],
     "cg_solver_get_config": [_P, _P],
     "cg_fft3d_create": [_I, _I, _I, _I, C.POINTER(_P)],
     "cg_fft3d_destroy": [_P],

@@ -443,7 +443,14 @@ struct ZPShape {
   static constexpr int EX_I = RowEx<A, B>::SLAB, EX_F = RowEx<B, A>::SLAB;
   static constexpr int EX = EX_I > EX_F ? EX_I : EX_F;
   static constexpr int B_STG = NH * 34, B_EX = CG_TILE * EX, B_XB = N * 17;  // float2 units
-  static constexpr int B_MAX = B_STG > B_EX ? (B_STG > B_XB ? B_STG : B_XB) : (B_EX > B_XB ? B_EX : B_XB);
+  // tensor-map staging: two 128-byte-wide boxes (8 pencils each) of NH k
+  // rows, each on a 1024-byte boundary (the 128-byte swizzle repeats every 8
+  // rows), plus 1024 bytes to align the first one inside the item buffer
+  static constexpr bool TMA_OK = NH <= 256;
+  static constexpr int BOXB = (NH * 128 + 1023) / 1024 * 1024;
+  static constexpr int B_TMA = TMA_OK ? (2 * BOXB + 1024) / 8 : 0;
+  static constexpr int B_MAX0 = B_STG > B_EX ? (B_STG > B_XB ? B_STG : B_XB) : (B_EX > B_XB ? B_EX : B_XB);
+  static constexpr int B_MAX = B_MAX0 > B_TMA ? B_MAX0 : B_TMA;
   static constexpr int BUF = (B_MAX + 1) / 2 * 2;  // even: float4-aligned
   // without the k_z and sponge tables: they stay in shared memory when
   // everything fits the 227 KB a CTA may hold, else they are read through L1
@@ -459,7 +466,9 @@ struct ZPShape {
   // (dt/rho, absorb) in the u-pass, in the same place
   static constexpr size_t OFF_TAB = OFF_BUF + 2 * (size_t)BUF;
   static constexpr size_t OFF_LAB = OFF_TAB + 2 * 256;
-  static constexpr size_t smem = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
+  // then the two staging mbarriers (bytes from the start)
+  static constexpr size_t OFF_BAR = sizeof(float2) * OFF_LAB + 2 * (size_t)CG_ZROWS * N;
+  static constexpr size_t smem = OFF_BAR + 2 * sizeof(unsigned long long);
   static_assert(smem <= LIMIT, "persistent z-pass tile does not fit shared memory");
 };
 
@@ -485,11 +494,11 @@ __device__ __forceinline__ void z_prefetch_labels(uint8_t* lab_s, const uint8_t*
   for (int i = threadIdx.x; i < n16; i += blockDim.x) cgf::cp_async16(lab_s + 16 * i, src + 16 * i);
 }
 
-// z_inputs on a raw staged tile: times i*mk[k] when mk is given, Im of the
-// self-paired bins dropped, then the Hermitian extension.
-template <int N>
-__device__ __forceinline__ void z_inputs_raw(float2 (&v)[ZSplit<N>::A], const float4* stg4, int p, int s,
-                                             const float* mk) {
+// z_inputs on a staged tile: times i*mk[k] when mk is given, Im of the
+// self-paired bins dropped, then the Hermitian extension. `row(k)` is the
+// staged float4 (A_k, B_k) of this thread's pencil.
+template <int N, class Row>
+__device__ __forceinline__ void z_inputs_from(float2 (&v)[ZSplit<N>::A], int s, const float* mk, Row row) {
   constexpr int A = ZSplit<N>::A, B = ZSplit<N>::B;
   static_for<0, A>([&](auto ai) {
     constexpr int a = decltype(ai)::value;
@@ -498,7 +507,7 @@ __device__ __forceinline__ void z_inputs_raw(float2 (&v)[ZSplit<N>::A], const fl
     if (s < B) {
       const bool hi = 2 * n > N;
       const int k = hi ? N - n : n;
-      const float4 f = stg4[k * 17 + p];
+      const float4 f = row(k);
       float2 fa = make_float2(f.x, f.y), fb = make_float2(f.z, f.w);
       if (mk) {
         const float kk = mk[k];
@@ -514,6 +523,13 @@ __device__ __forceinline__ void z_inputs_raw(float2 (&v)[ZSplit<N>::A], const fl
     }
     v[a] = z;
   });
+}
+
+// ... from the padded cp.async staging, stg4[k * 17 + p]
+template <int N>
+__device__ __forceinline__ void z_inputs_raw(float2 (&v)[ZSplit<N>::A], const float4* stg4, int p, int s,
+                                             const float* mk) {
+  z_inputs_from<N>(v, s, mk, [&](int k) { return stg4[k * 17 + p]; });
 }
 
 template <int N, bool UPASS>
@@ -537,11 +553,54 @@ __device__ __forceinline__ void zp_tables(float2* sm, const Tables& t, const Med
     }
 }
 
+// Tensor-map staging of item buffer j: its first 1024-byte boundary.
 template <int N>
+__device__ __forceinline__ char* zt_stage(float2* sm, int j) {
+  char* b = reinterpret_cast<char*>(sm + ZPShape<N>::OFF_BUF + (size_t)j * ZPShape<N>::BUF);
+  const unsigned a = cgf::smem_addr(b);
+  return b + (((a + 1023u) & ~1023u) - a);
+}
+
+// The half spectrum of tile (member b, x, y0) into item buffer j by two box
+// copies (pencils 0-7, 8-15), counted on bar; issued by one thread.
+template <int N>
+__device__ __forceinline__ void zt_issue(float2* sm, int j, unsigned long long* bar, const CUtensorMap* map,
+                                         const Dims& d, long long b, int x, int y0) {
+  using Z = ZPShape<N>;
+  char* dst = zt_stage<N>(sm, j);
+  const int c2 = (int)(b * d.nx + x);
+  cgf::mbar_expect_tx(bar, 2u * Z::NH * 128u);
+  cgf::tma_load_3d(dst, map, bar, 2 * y0, 0, c2);
+  cgf::tma_load_3d(dst + Z::BOXB, map, bar, 2 * y0 + 32, 0, c2);
+}
+
+// z_inputs from the tensor-map staging: pencil p's 16 bytes of row k sit in
+// box p / 8 at chunk (p % 8) XOR (k % 8) of the row's 128 bytes.
+template <int N>
+__device__ __forceinline__ void z_inputs_tma(float2 (&v)[ZSplit<N>::A], const char* stg, int p, int s,
+                                             const float* mk) {
+  const char* box = stg + (p >> 3) * ZPShape<N>::BOXB;
+  const int c = p & 7;
+  z_inputs_from<N>(v, s, mk,
+                   [&](int k) { return *reinterpret_cast<const float4*>(box + k * 128 + ((c ^ (k & 7)) << 4)); });
+}
+
+// Waits for item buffer j's staging (tensor-map path); a wait that gives up
+// raises the flag and the kernel carries on with whatever arrived.
+__device__ __forceinline__ void zt_wait(unsigned long long* bars, unsigned& phase, int j, const ZTma* ztma) {
+  if (!cgf::mbar_wait(bars + j, (phase >> j) & 1u)) atomicExch(ztma->err, 1);
+  phase ^= 1u << j;
+}
+
+// TMA: the tile's half spectra arrive by tensor-map box copies on an
+// mbarrier (ztma, descriptors in device memory) instead of per-thread
+// cp.async; the labels keep cp.async.
+template <int N, bool TMA = false>
 __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpass_u(Dims d, Tables t, MediumDev m,
                                                                        float* __restrict__ u, float2* __restrict__ S0,
                                                                        float2* __restrict__ S1, float2* __restrict__ S2,
-                                                                       int n_members, int tiles_per_cta) {
+                                                                       int n_members, int tiles_per_cta,
+                                                                       const ZTma* __restrict__ ztma) {
   using Z = ZPShape<N>;
   constexpr int A = Z::A, B = Z::B;
   extern __shared__ float2 sm[];
@@ -552,6 +611,16 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   const long long t1 = min(total, t0 + tiles_per_cta);
   cgf::pdl_trigger();
   if (t0 >= t1) return;  // the whole CTA, before any barrier
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(sm) + Z::OFF_BAR);
+  unsigned phase = 0u;  // bit j: parity of item buffer j's next staging phase
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      cgf::mbar_init(bars, 1);
+      cgf::mbar_init(bars + 1, 1);
+      cgf::mbar_init_fence();
+    }
+    __syncthreads();
+  }
   zp_tables<N, true>(sm, t, m);
   cgf::pdl_wait();
   const float* kz_s = Z::TBL ? reinterpret_cast<const float*>(sm + Z::OFF_KZ) : t.kz;
@@ -567,7 +636,11 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   auto prefetch = [&](long long tile, int comp, int j) {
     const long long b = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
-    z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), spec(comp, b), d, x, y0);
+    if constexpr (TMA) {
+      if (threadIdx.x == 0) zt_issue<N>(sm, j, bars + j, &ztma->map[comp], d, b, x, y0);  // map order = comp order
+    } else {
+      z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), spec(comp, b), d, x, y0);
+    }
     if (comp == 0 && lab && (tile == t0 || b == 0))
       z_prefetch_labels<N>(lab0 + label_slot(tile) * CG_ZROWS * N, m.labels, d, x, y0);
     cgf::cp_async_commit();
@@ -599,6 +672,9 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
         });
       };
       if (Z::EARLY) load_u();
+      // (tensor-map path) this thread's generic accesses to the buffer the
+      // next copy fills are ordered before that copy
+      if constexpr (TMA) cgf::fence_proxy_async();
       cgf::cp_async_wait0();
       __syncthreads();
       {
@@ -612,7 +688,12 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       }
       float2* bufj = sm + Z::OFF_BUF + (size_t)j * Z::BUF;
       float2 v[A], w[B];
-      z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, comp == 2 ? kz_s : nullptr);
+      if constexpr (TMA) {
+        zt_wait(bars, phase, j, ztma);
+        z_inputs_tma<N>(v, zt_stage<N>(sm, j), p, s, comp == 2 ? kz_s : nullptr);
+      } else {
+        z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, comp == 2 ? kz_s : nullptr);
+      }
       __syncthreads();  // the staging is read: the buffer becomes the exchange
       const RowEx<A, B, Z::WARP> exi{bufj + p * Z::EX};
       const RowEx<B, A, Z::WARP> exf{bufj + p * Z::EX};
@@ -650,15 +731,18 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
 // FWD: only the closing forward transform, of the pressure as it is -- the
 // spectrum a step leaves behind, rebuilt from a restored pressure field by
 // the very code the step runs, so a restored run continues bit for bit.
-template <int N, bool REC, bool FWD = false>
+// TMA: the half spectra arrive by tensor-map box copies (as in the u-pass).
+template <int N, bool REC, bool FWD = false, bool TMA = false>
 __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpass_p(Dims d, Tables t, MediumDev m,
                                                                        SourceDev src, RecordDev rec,
                                                                        const long long* ctl, int n_local, int record,
                                                                        float* __restrict__ p_all,
                                                                        float2* __restrict__ S0, int n_members,
-                                                                       int tiles_per_cta) {
+                                                                       int tiles_per_cta,
+                                                                       const ZTma* __restrict__ ztma) {
   using Z = ZPShape<N>;
   constexpr int A = Z::A, B = Z::B;
+  static_assert(!(FWD && TMA), "the forward-only pass stages no spectrum");
   extern __shared__ float2 sm[];
   const int ytiles = (d.ny + CG_ZROWS - 1) / CG_ZROWS;  // ny even; the last tile may be ragged
   const long long per_member = (long long)d.nx * ytiles;
@@ -667,6 +751,16 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   const long long t1 = min(total, t0 + tiles_per_cta);
   cgf::pdl_trigger();
   if (t0 >= t1) return;  // the whole CTA, before any barrier
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(sm) + Z::OFF_BAR);
+  unsigned phase = 0u;  // bit j: parity of item buffer j's next staging phase
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      cgf::mbar_init(bars, 1);
+      cgf::mbar_init(bars + 1, 1);
+      cgf::mbar_init_fence();
+    }
+    __syncthreads();
+  }
   zp_tables<N, false>(sm, t, m);
   cgf::pdl_wait();
   const float* sz_s = Z::TBL ? reinterpret_cast<const float*>(sm + Z::OFF_SZ) : t.sz;
@@ -680,7 +774,11 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
   auto prefetch = [&](long long tile, int j) {
     const long long b = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
-    z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), S0 + b * d.nspec, d, x, y0);
+    if constexpr (TMA) {
+      if (threadIdx.x == 0) zt_issue<N>(sm, j, bars + j, &ztma->map[1], d, b, x, y0);  // map[1]: S0
+    } else {
+      z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), S0 + b * d.nspec, d, x, y0);
+    }
     if (lab && (tile == t0 || b == 0)) z_prefetch_labels<N>(lab0 + label_slot(tile) * CG_ZROWS * N, m.labels, d, x, y0);
     cgf::cp_async_commit();
   };
@@ -745,6 +843,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       });
     };
     if (Z::EARLY) load_p();
+    if constexpr (TMA) cgf::fence_proxy_async();  // see the u-pass
     cgf::cp_async_wait0();
     __syncthreads();
     if (tile + 1 < t1) prefetch(tile + 1, j ^ 1);
@@ -752,7 +851,12 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const uint8_t* la = lab0 + label_slot(tile) * CG_ZROWS * N + (2 * p) * N;
     const uint8_t* lb = la + N;
     float2 v[A], w[B];
-    z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, nullptr);
+    if constexpr (TMA) {
+      zt_wait(bars, phase, j, ztma);
+      z_inputs_tma<N>(v, zt_stage<N>(sm, j), p, s, nullptr);
+    } else {
+      z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, nullptr);
+    }
     __syncthreads();  // the staging is read: the buffer becomes the exchange
     const RowEx<A, B, Z::WARP> exi{bufj + p * Z::EX};
     const RowEx<B, A, Z::WARP> exf{bufj + p * Z::EX};
@@ -883,27 +987,49 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
 }
 
 // ------------------------------------------------ per-length launchers --
-// persistent z-passes (any N of CG_FAST_ZSIZES, ny even)
+// persistent z-passes (any N of CG_FAST_ZSIZES, ny even); ztma (device
+// descriptors) selects the tensor-map staging where the length allows it
 template <int N>
 void zp_run_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
-              int batch, cudaStream_t st) {
+              int batch, cudaStream_t st, const ZTma* ztma) {
   int g = 0, per = 0;
   cgf::persistent_grid((long long)d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS) * batch, ZPShape<N>::MINB, &g, &per);
+  if constexpr (ZPShape<N>::TMA_OK) {
+    if (ztma) {
+      cgf::launch(kfp_zpass_u<N, true>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, u, S0, S1,
+                  S2, batch, per, ztma);
+      return;
+    }
+  }
   cgf::launch(kfp_zpass_u<N>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, u, S0, S1, S2,
-              batch, per);
+              batch, per, (const ZTma*)nullptr);
 }
 
 template <int N>
 void zp_run_p(const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src, const RecordDev& rec,
-              const long long* ctl, int n_local, int record, float* p, float2* S0, int batch, cudaStream_t st) {
+              const long long* ctl, int n_local, int record, float* p, float2* S0, int batch, cudaStream_t st,
+              const ZTma* ztma) {
   int g = 0, per = 0;
   cgf::persistent_grid((long long)d.nx * ((d.ny + CG_ZROWS - 1) / CG_ZROWS) * batch, ZPShape<N>::MINB, &g, &per);
+  const dim3 grid(g), block(ZPShape<N>::THREADS);
+  const size_t sm = ZPShape<N>::smem;
+  if constexpr (ZPShape<N>::TMA_OK) {
+    if (ztma) {
+      if (record)
+        cgf::launch(kfp_zpass_p<N, true, false, true>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record, p,
+                    S0, batch, per, ztma);
+      else
+        cgf::launch(kfp_zpass_p<N, false, false, true>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record,
+                    p, S0, batch, per, ztma);
+      return;
+    }
+  }
   if (record)
-    cgf::launch(kfp_zpass_p<N, true>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, src, rec,
-                ctl, n_local, record, p, S0, batch, per);
+    cgf::launch(kfp_zpass_p<N, true>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record, p, S0, batch, per,
+                (const ZTma*)nullptr);
   else
-    cgf::launch(kfp_zpass_p<N, false>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, src, rec,
-                ctl, n_local, record, p, S0, batch, per);
+    cgf::launch(kfp_zpass_p<N, false>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record, p, S0, batch,
+                per, (const ZTma*)nullptr);
 }
 
 template <int N>
@@ -917,19 +1043,23 @@ void zp_run_fwd(const Dims& d, const Tables& t, const MediumDev& m, float* p, fl
   memset(&rec, 0, sizeof(rec));
   rec.spp = 1;
   cgf::launch(kfp_zpass_p<N, false, true>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, src,
-              rec, (const long long*)nullptr, 0, 0, p, S0, batch, per);
+              rec, (const long long*)nullptr, 0, 0, p, S0, batch, per, (const ZTma*)nullptr);
+}
+
+template <typename K>
+static bool zp_allow(K kernel, int bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess;
 }
 
 template <int N>
 int zp_prepare() {
   const int sm = (int)ZPShape<N>::smem;
-  return (cudaFuncSetAttribute(kfp_zpass_u<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
-          cudaFuncSetAttribute(kfp_zpass_p<N, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) !=
-              cudaSuccess ||
-          cudaFuncSetAttribute(kfp_zpass_p<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess ||
-          cudaFuncSetAttribute(kfp_zpass_p<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
-             ? -1
-             : 0;
+  bool ok = zp_allow(kfp_zpass_u<N>, sm) && zp_allow(kfp_zpass_p<N, false, true>, sm) &&
+            zp_allow(kfp_zpass_p<N, true>, sm) && zp_allow(kfp_zpass_p<N, false>, sm);
+  if constexpr (ZPShape<N>::TMA_OK)
+    ok = ok && zp_allow(kfp_zpass_u<N, true>, sm) && zp_allow(kfp_zpass_p<N, true, false, true>, sm) &&
+         zp_allow(kfp_zpass_p<N, false, false, true>, sm);
+  return ok ? 0 : -1;
 }
 
 // one-tile-per-CTA z-passes (N of CG_FAST_SIZES, any ny)
@@ -968,9 +1098,9 @@ int zt_prepare() {
 
 #define CG_ZP_INSTANTIATE(n)                                                                                       \
   template void zp_run_u<n>(const Dims&, const Tables&, const MediumDev&, float*, float2*, float2*, float2*, int,  \
-                            cudaStream_t);                                                                         \
+                            cudaStream_t, const ZTma*);                                                            \
   template void zp_run_p<n>(const Dims&, const Tables&, const MediumDev&, const SourceDev&, const RecordDev&,     \
-                            const long long*, int, int, float*, float2*, int, cudaStream_t);                      \
+                            const long long*, int, int, float*, float2*, int, cudaStream_t, const ZTma*);         \
   template void zp_run_fwd<n>(const Dims&, const Tables&, const MediumDev&, float*, float2*, int, cudaStream_t); \
   template int zp_prepare<n>();
 #define CG_ZT_INSTANTIATE(n)                                                                                       \

@@ -655,6 +655,21 @@ static void invalidate_graphs(cg_solver* s) {
     }
 }
 
+// The tensor-map staging flag: CG_ERR_TIMEOUT when a z-pass gave up waiting
+// for a staged tile since the handle was created (its results are not to be
+// trusted). Synchronises the handle's stream; free when the staging is off.
+static int ztma_check(cg_solver* s) {
+  if (!s->ztma_err) return CG_OK;
+  int v = 0;
+  CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  CG_CUDA_TRY(cudaMemcpy(&v, s->ztma_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) {
+    cg_set_error("a z-pass gave up waiting for a tensor-map copy of its tile");
+    return CG_ERR_TIMEOUT;
+  }
+  return CG_OK;
+}
+
 template <typename T>
 static int dev_alloc(T** p, size_t count) {
   if (count == 0) count = 1;
@@ -680,7 +695,7 @@ static void solver_free(cg_solver* s) {
   void* ptrs[] = {s->p, s->u, s->S0, s->S1, s->S2, s->twx, s->twy, s->twz, s->kx, s->ky, s->kz, s->kx2, s->ky2,
                   s->kz2, s->sx, s->sy, s->sz, s->labels, s->ltab, s->dtr, s->rc2, s->ab, s->b2, s->src_ptr,
                   s->src_z, s->src_ac, s->src_as, s->drive, s->bins, s->comp, s->pmax, s->peaks, s->harm_dev,
-                  s->ctl, s->ph, s->post};
+                  s->ctl, s->ph, s->post, s->ztma_dev};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -809,6 +824,26 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
     cg_set_error("cudaStreamCreate: %s", cudaGetErrorString(e));
     solver_free(s);
     return CG_ERR_CUDA;
+  }
+  // tensor-map descriptors of the three spectra for the persistent
+  // z-passes, in device memory with the staging flag behind them; a grid the
+  // driver refuses them for keeps the cp.async staging
+  if (ztma_supported(s->d)) {
+    ZTma host;
+    memset(&host, 0, sizeof(host));
+    char* buf = nullptr;
+    if (ztma_encode(&host, s->d, s->B, s->S1, s->S0, s->S2) == CG_OK &&
+        cudaMalloc(&buf, sizeof(ZTma) + 64) == cudaSuccess) {
+      host.err = reinterpret_cast<int*>(buf + sizeof(ZTma));
+      if (cudaMemcpy(buf, &host, sizeof(ZTma), cudaMemcpyHostToDevice) == cudaSuccess &&
+          cudaMemset(host.err, 0, sizeof(int)) == cudaSuccess) {
+        s->ztma_dev = reinterpret_cast<ZTma*>(buf);
+        s->ztma_err = host.err;
+      } else {
+        cudaFree(buf);
+      }
+    }
+    cudaGetLastError();
   }
   cudaStream_t st = s->stream;
   k_twiddles<<<(cfg->nx + 255) / 256, 256, 0, st>>>(s->twx, cfg->nx);
@@ -1149,7 +1184,9 @@ static int launch_step(cg_solver* s, int n_local, int record, EvLog* log = nullp
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
   }
   mark(3);
-  if (!fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, s->zpers != 0))
+  const ZTma* zt = (s->ztma && s->zpers) ? s->ztma_dev : nullptr;
+  if (!(zt && fast_zpass_u_tma(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, zt)) &&
+      !fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, s->zpers != 0))
     k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
   if (fx) {
     mark(4);
@@ -1169,7 +1206,9 @@ static int launch_step(cg_solver* s, int n_local, int record, EvLog* log = nullp
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV, d, s->py, t, s->S0, s->S1, s->S2);
   }
   mark(7);
-  if (!fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st,
+  if (!(zt && fast_zpass_p_tma(d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B,
+                               st, zt)) &&
+      !fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st,
                     s->zpers != 0))
     k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
                                                  record, s->p, s->S0);
@@ -1252,6 +1291,10 @@ extern "C" int cg_solver_read_peaks(cg_solver* s, int first, int count, float* o
   CG_REQUIRE(s && out, "null argument");
   CG_REQUIRE(first >= 0 && count >= 0 && first + count <= s->max_periods, "period range out of bounds");
   CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (s->ztma) {
+    const int rc = ztma_check(s);
+    if (rc != CG_OK) return rc;
+  }
   for (int b = 0; b < s->B; ++b)
     CG_CUDA_TRY(cudaMemcpy(out + (size_t)b * count, s->peaks + (size_t)b * s->max_periods + first,
                            sizeof(float) * count, cudaMemcpyDefault));
@@ -1280,7 +1323,7 @@ extern "C" int cg_solver_finalize(cg_solver* s, int n_record_steps, float* phaso
     return CG_ERR_CUDA;
   }
   s->ph_valid = 1;
-  return CG_OK;
+  return s->ztma ? ztma_check(s) : CG_OK;
 }
 
 int cg_solver_post_scratch(cg_solver* s, size_t bytes) {
@@ -1364,6 +1407,7 @@ extern "C" int cg_solver_timed_run(cg_solver* s, int n_steps, int record, int gr
   CG_CUDA_TRY(cudaEventElapsedTime(ms, a, b));
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  if (rc == CG_OK && s->ztma) rc = ztma_check(s);
   return rc;
 }
 
@@ -1384,7 +1428,7 @@ struct TuneKey {
   }
 };
 struct TuneChoice {
-  int fused, zpers, slabs;
+  int fused, zpers, slabs, ztma;
 };
 std::map<TuneKey, TuneChoice> g_tuned;
 std::mutex g_tune_mu;
@@ -1429,6 +1473,7 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
       s->fused_xy = it->second.fused;
       s->zpers = it->second.zpers;
       s->slabs = it->second.slabs;
+      s->ztma = (it->second.ztma && s->ztma_dev) ? 1 : 0;
       out4[0] = s->fused_xy;
       out4[1] = s->zpers;
       out4[2] = 0;
@@ -1449,23 +1494,29 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   // process tunes while other solves run) cannot hand the choice to a
   // slower configuration.
   constexpr int kRounds = 3;
-  constexpr int kMaxCand = 4 + CG_MAX_SLABS;
+  constexpr int kMaxCand = 8 + CG_MAX_SLABS;
   TuneChoice cand[kMaxCand];
   float cand_ms[kMaxCand];
   int nc = 0;
+  // CG_ZTMA=0 / =1 keep the persistent z-tiles on cp.async / on tensor-map
+  // staging (where the grid allows it); unset, both are timed
+  const char* tenv_z = getenv("CG_ZTMA");
+  const int zt_lo = (s->ztma_dev && tenv_z && tenv_z[0] == '1') ? 1 : 0;
+  const int zt_hi = (s->ztma_dev && !(tenv_z && tenv_z[0] == '0')) ? 1 : 0;
   if (slab_pinned) {
     const int k = atoi(senv);
-    cand[nc++] = {0, 1, (k > 1 && slabs_supported(s->d)) ? (k > CG_MAX_SLABS ? CG_MAX_SLABS : k) : 1};
+    cand[nc++] = {0, 1, (k > 1 && slabs_supported(s->d)) ? (k > CG_MAX_SLABS ? CG_MAX_SLABS : k) : 1, 0};
   } else {
     for (int fx = fx_lo; fx <= (fx_ok ? 1 : 0); ++fx)
-      for (int zp = 1; zp >= (zp_choice ? 0 : 1); --zp) cand[nc++] = {fx, zp, 1};
+      for (int zp = 1; zp >= (zp_choice ? 0 : 1); --zp)
+        for (int zt = (zp ? zt_lo : 0); zt <= (zp ? zt_hi : 0); ++zt) cand[nc++] = {fx, zp, 1, zt};
     // slab counts join the candidates only on request (CG_TUNE_SLABS=1): on
     // GB300 they measured slower than the plain step on every grid tried
     const char* tenv = getenv("CG_TUNE_SLABS");
     if (!(fenv && fenv[0] == '1') && tenv && tenv[0] == '1') {
       int ks[CG_MAX_SLABS];
       const int nk = slab_candidates(s, ks);
-      for (int i = 0; i < nk; ++i) cand[nc++] = {0, 1, ks[i]};
+      for (int i = 0; i < nk; ++i) cand[nc++] = {0, 1, ks[i], 0};
     }
   }
   for (int c = 0; c < nc; ++c) cand_ms[c] = 1e30f;
@@ -1474,6 +1525,7 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
       s->fused_xy = cand[c].fused;
       s->zpers = cand[c].zpers;
       s->slabs = cand[c].slabs;
+      s->ztma = cand[c].ztma;
       int rc = CG_OK;
       for (int k = 0; k < (r == 0 ? 2 : 1) && rc == CG_OK; ++k) rc = launch_step(s, k % s->spp, 0);
       CG_CUDA_TRY(cudaEventRecord(a, s->stream));
@@ -1501,7 +1553,10 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   s->fused_xy = best.fused;
   s->zpers = best.zpers;
   s->slabs = best.slabs;
-  int rc = cg_solver_reset(s);
+  s->ztma = best.ztma;
+  int rc = ztma_check(s);
+  if (rc != CG_OK) return rc;
+  rc = cg_solver_reset(s);
   if (rc != CG_OK) return rc;
   if (!pinned) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1530,6 +1585,26 @@ extern "C" int cg_solver_set_slabs(cg_solver* s, int slabs) {
   const int rc = spectrum_from_pressure(s);
   if (rc != CG_OK) return rc;
   CG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return CG_OK;
+}
+
+extern "C" int cg_solver_set_zstaging(cg_solver* s, int tma) {
+  CG_REQUIRE(s, "null solver");
+  CG_REQUIRE(tma == 0 || tma == 1, "tma must be 0 or 1, got %d", tma);
+  CG_REQUIRE(!tma || s->ztma_dev,
+             "tensor-map staging needs persistent z-passes with nz / 2 + 1 <= 256 and an even ny (grid %dx%dx%d)",
+             s->d.nx, s->d.ny, s->d.nz);
+  CG_REQUIRE(!tma || s->slabs == 1, "tensor-map staging runs the plain step only (slabs = %d)", s->slabs);
+  if (tma == s->ztma && (!tma || s->zpers)) return CG_OK;
+  invalidate_graphs(s);
+  if (tma) s->zpers = 1;
+  s->ztma = tma;
+  return CG_OK;
+}
+
+extern "C" int cg_solver_get_zstaging(const cg_solver* s, int* tma) {
+  CG_REQUIRE(s && tma, "null argument");
+  *tma = (s->ztma && s->zpers && s->slabs == 1) ? 1 : 0;
   return CG_OK;
 }
 

@@ -2,6 +2,8 @@
 // size-specialised translation units).
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (types only: the encoder is reached through the runtime)
+
 #include "cg_common.cuh"
 
 // ------------------------------------------------------------ structures --
@@ -122,6 +124,30 @@ bool fast_zpass_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, 
 bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src,
                   const RecordDev& rec, const long long* ctl, int n_local, int record, float* p, float2* S0,
                   int batch, cudaStream_t st, bool persistent = true);
+
+// Tensor-map (TMA) staging of the persistent z-tiles: one descriptor per
+// spectrum in the u-pass's component order (S1, S0, S2; the p-pass reads
+// map[1] = S0), each a [member x][kz][2 ny floats] grid of 32-float x kz
+// boxes, and a device flag that a staging wait sets if it gives up. The
+// kernels read the descriptors from global memory (written once by the host
+// before any launch that uses them).
+struct ZTma {
+  CUtensorMap map[3];
+  int* err;
+};
+// 1 when the persistent z-passes of this grid can stage by tensor map: ny
+// even, nz one of their lengths with nz / 2 + 1 <= 256 (a box dimension)
+int ztma_supported(const Dims& d);
+// Encode the three descriptors for `batch` members into *z (host memory);
+// CG_OK, or an error (set) when the driver refuses them.
+int ztma_encode(ZTma* z, const Dims& d, int batch, float2* S1, float2* S0, float2* S2);
+// u- and p-passes staged by tensor map (persistent kernels; z_dev: the
+// descriptors in device memory). False when the grid has no such kernel.
+bool fast_zpass_u_tma(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1,
+                      float2* S2, int batch, cudaStream_t st, const ZTma* z_dev);
+bool fast_zpass_p_tma(const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src, const RecordDev& rec,
+                      const long long* ctl, int n_local, int record, float* p, float2* S0, int batch,
+                      cudaStream_t st, const ZTma* z_dev);
 
 // The forward z-transform of p into S0 with the kernel family the step's
 // p-pass runs on this grid (bitwise the spectrum a step leaves); false when

@@ -44,6 +44,12 @@ struct cg_solver {
   // each slab's spectra and fields stay in L2 between its three passes; the
   // pressure spectrum between steps is then y- and z-transformed
   int slabs = 1;
+  // tensor-map staging of the persistent z-tiles: descriptors of S1, S0, S2
+  // in device memory (null where the grid does not allow it), the flag a
+  // staging wait raises when it gives up, and whether the step uses it
+  ZTma* ztma_dev = nullptr;
+  int* ztma_err = nullptr;
+  int ztma = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one period, record off/on
   // phasors of the last finalize, [B][nh][nrec], kept for device post-processing
   float2* ph = nullptr;

@@ -570,7 +570,8 @@ class DeviceSolver:
             cfg4 = np.zeros(4, np.int32)
             _lib.call("cg_solver_get_config", h, _lib.ptr(cfg4))
             self.tuning = {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]), "slabs": int(cfg4[2]),
-                           "configurations_timed": int(out[2]), "cached": bool(out[3])}
+                           "tma_staging": self._zstaging(), "configurations_timed": int(out[2]),
+                           "cached": bool(out[3])}
         info = np.zeros(8, np.int64)
         _lib.call("cg_solver_info", h, _lib.ptr(info))
         self.nrec = int(info[2])
@@ -593,11 +594,20 @@ class DeviceSolver:
         _lib.call("cg_solver_info", self.h, _lib.ptr(info))
         self.launches_per_step = int(info[7])
 
+    def set_zstaging(self, tma: bool) -> None:
+        """Stage the persistent z-tiles by tensor-map copies (True) or cp.async (False); bit-identical results."""
+        _lib.call("cg_solver_set_zstaging", self.h, int(bool(tma)))
+
+    def _zstaging(self) -> bool:
+        v = C.c_int(0)
+        _lib.call("cg_solver_get_zstaging", self.h, C.byref(v))
+        return bool(v.value)
+
     def config(self) -> dict:
         out = np.zeros(4, np.int32)
         _lib.call("cg_solver_get_config", self.h, _lib.ptr(out))
         return {"fused_transverse": bool(out[0]), "persistent_z": bool(out[1]), "slabs": int(out[2]),
-                "launches_per_step": int(out[3])}
+                "launches_per_step": int(out[3]), "tma_staging": self._zstaging()}
 
     def extend_drive(self, n_steps: int) -> None:
         """Drive table covering ``n_steps`` steps (the default covers one solve's schedule)."""

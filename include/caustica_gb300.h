@@ -115,8 +115,10 @@ int cg_solver_profile(cg_solver* s, int n_steps, int record, float* ms8);
 int cg_solver_info(const cg_solver* s, long long* out8);
 /* Autotuner: on a fresh handle (medium, source and drive set) time each
  * launch configuration the grid admits -- cluster-fused or three-pass
- * transverse chain, persistent or one-tile-per-CTA z-passes (and slab
- * counts, cg_solver_set_slabs, when CG_TUNE_SLABS=1) -- over
+ * transverse chain, persistent or one-tile-per-CTA z-passes, cp.async or
+ * tensor-map staging of the persistent z-tiles (CG_ZTMA=0/1 pins it; see
+ * cg_solver_set_zstaging), and slab counts (cg_solver_set_slabs) when
+ * CG_TUNE_SLABS=1 -- over
  * n_steps steps of the handle itself, keep the fastest and reset the
  * handle's state. The choice is remembered per (grid, batch, physics,
  * medium storage) for the process; a batch of several members reuses the
@@ -134,6 +136,16 @@ int cg_solver_autotune(cg_solver* s, int n_steps, int* out4);
  * size-specialised passes on all three axes and an even ny. Synchronises.
  * No counterpart in the reference (it has one code path). */
 int cg_solver_set_slabs(cg_solver* s, int slabs);
+/* How the persistent z-passes stage a tile's half spectra in shared
+ * memory: 0 = 16-byte cp.async by every thread into padded rows; 1 = two
+ * tensor-map (TMA) box copies per tile, issued by one thread, completed on
+ * an mbarrier and read through the 128-byte swizzle (needs nz / 2 + 1 <=
+ * 256, an even ny and the plain step; tma = 1 also selects the persistent
+ * z-passes). Results are bit-identical either way. A staging wait that gives
+ * up (bounded) makes the next finalize, peak read or timed run return
+ * CG_ERR_TIMEOUT. No counterpart in the reference. */
+int cg_solver_set_zstaging(cg_solver* s, int tma);
+int cg_solver_get_zstaging(const cg_solver* s, int* tma);
 /* out4 = {cluster-fused transverse chain, persistent z-passes, slabs,
  * kernel launches per step} of the handle's current launch configuration. */
 int cg_solver_get_config(const cg_solver* s, int* out4);

@@ -35,6 +35,10 @@ def test_slot_symbols_name_the_dispatched_kernels():
     assert bench.slot_symbols((64, 63, 64))[3] == "kf_zpass_u<64>"
     assert bench.slot_symbols((64, 63, 320))[3] == "k_zpass_u"
     assert bench.slot_symbols((640, 64, 512))[1] == "kf_xpass<640,X_GRAD>"
+    # tensor-map staging of the persistent z-tiles (nz / 2 + 1 <= 256 only)
+    tma = bench.slot_symbols((192, 192, 256), tma=True)
+    assert tma[3] == "kfp_zpass_u<256,true>" and tma[7] == "kfp_zpass_p<256,false,false,true>"
+    assert bench.slot_symbols((64, 63, 64), tma=True)[3] == "kf_zpass_u<64>"
 
 
 def test_pennes_bytes_per_cell_substep():
