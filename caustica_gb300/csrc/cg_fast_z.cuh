@@ -425,8 +425,10 @@ __global__ void __launch_bounds__(CG_THREADS, CG_FAST_MINB) kf_zpass_p(Dims d, T
 // Persistent, pipelined z-passes (ny a multiple of the tile height). Each CTA
 // walks a contiguous run of tiles -- for the u-pass all three velocity
 // components of a tile in turn, so the tile's labels load once -- and the half
-// spectrum of the next (tile, component) streams into shared memory with
-// cp.async while the current one is transformed. An item's staging buffer is
+// spectrum of the next (tile, component) streams into shared memory -- by two
+// tensor-map box copies on an mbarrier (TMA instantiations) or by 16-byte
+// cp.async from every thread -- while the current one is transformed. An
+// item's staging buffer is
 // then reused as its exchange and split-store buffer, so the two buffers cost
 // what the single-item kernel's staging plus exchange cost and two CTAs still
 // fit on an SM.

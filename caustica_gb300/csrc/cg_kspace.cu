@@ -839,6 +839,7 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
           cudaMemset(host.err, 0, sizeof(int)) == cudaSuccess) {
         s->ztma_dev = reinterpret_cast<ZTma*>(buf);
         s->ztma_err = host.err;
+        s->ztma = 1;  // the default where it exists (measured faster on config 2); the tuner times both
       } else {
         cudaFree(buf);
       }
