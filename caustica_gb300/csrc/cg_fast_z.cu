@@ -118,18 +118,17 @@ int ztma_supported(const Dims& d) {
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
-// library links the static CUDA runtime only)
+// library links the static CUDA runtime only); looked up once, thread-safe
+// (handles are created from several host threads in a serving process)
 static PFN_cuTensorMapEncodeTiled_v12000 tensormap_encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void* f = nullptr;
     cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -162,12 +161,12 @@ int ztma_encode(ZTma* z, const Dims& d, int batch, float2* S1, float2* S0, float
 }
 
 bool fast_zpass_u_tma(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1,
-                      float2* S2, int batch, cudaStream_t st, const ZTma* z_dev) {
-  if (!ztma_supported(d) || !z_dev) return false;
+                      float2* S2, int batch, cudaStream_t st, const ZTma& z) {
+  if (!ztma_supported(d)) return false;
   switch (d.nz) {
 #define CASE(n)                                          \
   case n:                                                \
-    zp_run_u<n>(d, t, m, u, S0, S1, S2, batch, st, z_dev); \
+    zp_run_u<n>(d, t, m, u, S0, S1, S2, batch, st, &z);    \
     return true;
     CG_FAST_ZSIZES(CASE)
 #undef CASE
@@ -178,12 +177,12 @@ bool fast_zpass_u_tma(const Dims& d, const Tables& t, const MediumDev& m, float*
 
 bool fast_zpass_p_tma(const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src, const RecordDev& rec,
                       const long long* ctl, int n_local, int record, float* p, float2* S0, int batch,
-                      cudaStream_t st, const ZTma* z_dev) {
-  if (!ztma_supported(d) || !z_dev) return false;
+                      cudaStream_t st, const ZTma& z) {
+  if (!ztma_supported(d)) return false;
   switch (d.nz) {
 #define CASE(n)                                                                  \
   case n:                                                                        \
-    zp_run_p<n>(d, t, m, src, rec, ctl, n_local, record, p, S0, batch, st, z_dev); \
+    zp_run_p<n>(d, t, m, src, rec, ctl, n_local, record, p, S0, batch, st, &z);    \
     return true;
     CG_FAST_ZSIZES(CASE)
 #undef CASE

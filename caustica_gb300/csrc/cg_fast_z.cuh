@@ -589,20 +589,20 @@ __device__ __forceinline__ void z_inputs_tma(float2 (&v)[ZSplit<N>::A], const ch
 
 // Waits for item buffer j's staging (tensor-map path); a wait that gives up
 // raises the flag and the kernel carries on with whatever arrived.
-__device__ __forceinline__ void zt_wait(unsigned long long* bars, unsigned& phase, int j, const ZTma* ztma) {
-  if (!cgf::mbar_wait(bars + j, (phase >> j) & 1u)) atomicExch(ztma->err, 1);
+__device__ __forceinline__ void zt_wait(unsigned long long* bars, unsigned& phase, int j, int* err) {
+  if (!cgf::mbar_wait(bars + j, (phase >> j) & 1u)) atomicExch(err, 1);
   phase ^= 1u << j;
 }
 
 // TMA: the tile's half spectra arrive by tensor-map box copies on an
-// mbarrier (ztma, descriptors in device memory) instead of per-thread
-// cp.async; the labels keep cp.async.
+// mbarrier (ztma: the descriptors, by value) instead of per-thread cp.async;
+// the labels keep cp.async. Other instantiations ignore ztma.
 template <int N, bool TMA = false>
 __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpass_u(Dims d, Tables t, MediumDev m,
                                                                        float* __restrict__ u, float2* __restrict__ S0,
                                                                        float2* __restrict__ S1, float2* __restrict__ S2,
                                                                        int n_members, int tiles_per_cta,
-                                                                       const ZTma* __restrict__ ztma) {
+                                                                       const __grid_constant__ ZTma ztma) {
   using Z = ZPShape<N>;
   constexpr int A = Z::A, B = Z::B;
   extern __shared__ float2 sm[];
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const long long b = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     if constexpr (TMA) {
-      if (threadIdx.x == 0) zt_issue<N>(sm, j, bars + j, &ztma->map[comp], d, b, x, y0);  // map order = comp order
+      if (threadIdx.x == 0) zt_issue<N>(sm, j, bars + j, &ztma.map[comp], d, b, x, y0);  // map order = comp order
     } else {
       z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), spec(comp, b), d, x, y0);
     }
@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
       float2* bufj = sm + Z::OFF_BUF + (size_t)j * Z::BUF;
       float2 v[A], w[B];
       if constexpr (TMA) {
-        zt_wait(bars, phase, j, ztma);
+        zt_wait(bars, phase, j, ztma.err);
         z_inputs_tma<N>(v, zt_stage<N>(sm, j), p, s, comp == 2 ? kz_s : nullptr);
       } else {
         z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, comp == 2 ? kz_s : nullptr);
@@ -741,7 +741,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
                                                                        float* __restrict__ p_all,
                                                                        float2* __restrict__ S0, int n_members,
                                                                        int tiles_per_cta,
-                                                                       const ZTma* __restrict__ ztma) {
+                                                                       const __grid_constant__ ZTma ztma) {
   using Z = ZPShape<N>;
   constexpr int A = Z::A, B = Z::B;
   static_assert(!(FWD && TMA), "the forward-only pass stages no spectrum");
@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const long long b = tile % n_members, r = tile / n_members;
     const int x = (int)(r / ytiles), y0 = (int)(r - (long long)x * ytiles) * CG_ZROWS;
     if constexpr (TMA) {
-      if (threadIdx.x == 0) zt_issue<N>(sm, j, bars + j, &ztma->map[1], d, b, x, y0);  // map[1]: S0
+      if (threadIdx.x == 0) zt_issue<N>(sm, j, bars + j, &ztma.map[1], d, b, x, y0);  // map[1]: S0
     } else {
       z_prefetch<N>(reinterpret_cast<float4*>(sm + Z::OFF_BUF + (size_t)j * Z::BUF), S0 + b * d.nspec, d, x, y0);
     }
@@ -854,7 +854,7 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
     const uint8_t* lb = la + N;
     float2 v[A], w[B];
     if constexpr (TMA) {
-      zt_wait(bars, phase, j, ztma);
+      zt_wait(bars, phase, j, ztma.err);
       z_inputs_tma<N>(v, zt_stage<N>(sm, j), p, s, nullptr);
     } else {
       z_inputs_raw<N>(v, reinterpret_cast<const float4*>(bufj), p, s, nullptr);
@@ -989,8 +989,10 @@ __global__ void __launch_bounds__(ZPShape<N>::THREADS, ZPShape<N>::MINB) kfp_zpa
 }
 
 // ------------------------------------------------ per-length launchers --
-// persistent z-passes (any N of CG_FAST_ZSIZES, ny even); ztma (device
-// descriptors) selects the tensor-map staging where the length allows it
+// persistent z-passes (any N of CG_FAST_ZSIZES, ny even); ztma (encoded
+// descriptors, host memory) selects the tensor-map staging where the length
+// allows it
+static const ZTma kNoZTma = {};
 template <int N>
 void zp_run_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1, float2* S2,
               int batch, cudaStream_t st, const ZTma* ztma) {
@@ -999,12 +1001,12 @@ void zp_run_u(const Dims& d, const Tables& t, const MediumDev& m, float* u, floa
   if constexpr (ZPShape<N>::TMA_OK) {
     if (ztma) {
       cgf::launch(kfp_zpass_u<N, true>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, u, S0, S1,
-                  S2, batch, per, ztma);
+                  S2, batch, per, *ztma);
       return;
     }
   }
   cgf::launch(kfp_zpass_u<N>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, u, S0, S1, S2,
-              batch, per, (const ZTma*)nullptr);
+              batch, per, kNoZTma);
 }
 
 template <int N>
@@ -1019,19 +1021,19 @@ void zp_run_p(const Dims& d, const Tables& t, const MediumDev& m, const SourceDe
     if (ztma) {
       if (record)
         cgf::launch(kfp_zpass_p<N, true, false, true>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record, p,
-                    S0, batch, per, ztma);
+                    S0, batch, per, *ztma);
       else
         cgf::launch(kfp_zpass_p<N, false, false, true>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record,
-                    p, S0, batch, per, ztma);
+                    p, S0, batch, per, *ztma);
       return;
     }
   }
   if (record)
     cgf::launch(kfp_zpass_p<N, true>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record, p, S0, batch, per,
-                (const ZTma*)nullptr);
+                kNoZTma);
   else
     cgf::launch(kfp_zpass_p<N, false>, grid, block, sm, st, d, t, m, src, rec, ctl, n_local, record, p, S0, batch,
-                per, (const ZTma*)nullptr);
+                per, kNoZTma);
 }
 
 template <int N>
@@ -1045,7 +1047,7 @@ void zp_run_fwd(const Dims& d, const Tables& t, const MediumDev& m, float* p, fl
   memset(&rec, 0, sizeof(rec));
   rec.spp = 1;
   cgf::launch(kfp_zpass_p<N, false, true>, dim3(g), dim3(ZPShape<N>::THREADS), ZPShape<N>::smem, st, d, t, m, src,
-              rec, (const long long*)nullptr, 0, 0, p, S0, batch, per, (const ZTma*)nullptr);
+              rec, (const long long*)nullptr, 0, 0, p, S0, batch, per, kNoZTma);
 }
 
 template <typename K>

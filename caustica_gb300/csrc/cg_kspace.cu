@@ -695,7 +695,7 @@ static void solver_free(cg_solver* s) {
   void* ptrs[] = {s->p, s->u, s->S0, s->S1, s->S2, s->twx, s->twy, s->twz, s->kx, s->ky, s->kz, s->kx2, s->ky2,
                   s->kz2, s->sx, s->sy, s->sz, s->labels, s->ltab, s->dtr, s->rc2, s->ab, s->b2, s->src_ptr,
                   s->src_z, s->src_ac, s->src_as, s->drive, s->bins, s->comp, s->pmax, s->peaks, s->harm_dev,
-                  s->ctl, s->ph, s->post, s->ztma_dev};
+                  s->ctl, s->ph, s->post, s->ztma_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -826,22 +826,19 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
     return CG_ERR_CUDA;
   }
   // tensor-map descriptors of the three spectra for the persistent
-  // z-passes, in device memory with the staging flag behind them; a grid the
-  // driver refuses them for keeps the cp.async staging
+  // z-passes (launches pass them by value) and the staging flag on the
+  // device; a grid the driver refuses them for keeps the cp.async staging
   if (ztma_supported(s->d)) {
-    ZTma host;
-    memset(&host, 0, sizeof(host));
-    char* buf = nullptr;
-    if (ztma_encode(&host, s->d, s->B, s->S1, s->S0, s->S2) == CG_OK &&
-        cudaMalloc(&buf, sizeof(ZTma) + 64) == cudaSuccess) {
-      host.err = reinterpret_cast<int*>(buf + sizeof(ZTma));
-      if (cudaMemcpy(buf, &host, sizeof(ZTma), cudaMemcpyHostToDevice) == cudaSuccess &&
-          cudaMemset(host.err, 0, sizeof(int)) == cudaSuccess) {
-        s->ztma_dev = reinterpret_cast<ZTma*>(buf);
-        s->ztma_err = host.err;
+    int* flag = nullptr;
+    if (ztma_encode(&s->ztma_host, s->d, s->B, s->S1, s->S0, s->S2) == CG_OK &&
+        cudaMalloc(&flag, sizeof(int)) == cudaSuccess) {
+      if (cudaMemset(flag, 0, sizeof(int)) == cudaSuccess) {
+        s->ztma_host.err = flag;
+        s->ztma_err = flag;
+        s->ztma_ok = 1;
         s->ztma = 1;  // the default where it exists (measured faster on config 2); the tuner times both
       } else {
-        cudaFree(buf);
+        cudaFree(flag);
       }
     }
     cudaGetLastError();
@@ -1185,8 +1182,8 @@ static int launch_step(cg_solver* s, int n_local, int record, EvLog* log = nullp
       k_ypass<<<gy, CG_THREADS, s->smem_y, st>>>(Y_INV_GRAD, d, s->py, t, s->S0, s->S1, s->S2);
   }
   mark(3);
-  const ZTma* zt = (s->ztma && s->zpers) ? s->ztma_dev : nullptr;
-  if (!(zt && fast_zpass_u_tma(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, zt)) &&
+  const bool zt = s->ztma && s->zpers && s->ztma_ok;
+  if (!(zt && fast_zpass_u_tma(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, s->ztma_host)) &&
       !fast_zpass_u(d, t, m, s->u, s->S0, s->S1, s->S2, B, st, s->zpers != 0))
     k_zpass_u<<<gz, CG_THREADS, s->smem_z, st>>>(d, s->pz, t, m, s->u, s->S0, s->S1, s->S2);
   if (fx) {
@@ -1208,7 +1205,7 @@ static int launch_step(cg_solver* s, int n_local, int record, EvLog* log = nullp
   }
   mark(7);
   if (!(zt && fast_zpass_p_tma(d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B,
-                               st, zt)) &&
+                               st, s->ztma_host)) &&
       !fast_zpass_p(1, d, t, m, make_source(s), make_record(s), s->ctl, n_local, record, s->p, s->S0, B, st,
                     s->zpers != 0))
     k_zpass_p<<<gz, CG_THREADS, s->smem_z, st>>>(1, d, s->pz, t, m, make_source(s), make_record(s), s->ctl, n_local,
@@ -1474,7 +1471,7 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
       s->fused_xy = it->second.fused;
       s->zpers = it->second.zpers;
       s->slabs = it->second.slabs;
-      s->ztma = (it->second.ztma && s->ztma_dev) ? 1 : 0;
+      s->ztma = (it->second.ztma && s->ztma_ok) ? 1 : 0;
       out4[0] = s->fused_xy;
       out4[1] = s->zpers;
       out4[2] = 0;
@@ -1502,8 +1499,8 @@ extern "C" int cg_solver_autotune(cg_solver* s, int n_steps, int* out4) {
   // CG_ZTMA=0 / =1 keep the persistent z-tiles on cp.async / on tensor-map
   // staging (where the grid allows it); unset, both are timed
   const char* tenv_z = getenv("CG_ZTMA");
-  const int zt_lo = (s->ztma_dev && tenv_z && tenv_z[0] == '1') ? 1 : 0;
-  const int zt_hi = (s->ztma_dev && !(tenv_z && tenv_z[0] == '0')) ? 1 : 0;
+  const int zt_lo = (s->ztma_ok && tenv_z && tenv_z[0] == '1') ? 1 : 0;
+  const int zt_hi = (s->ztma_ok && !(tenv_z && tenv_z[0] == '0')) ? 1 : 0;
   if (slab_pinned) {
     const int k = atoi(senv);
     cand[nc++] = {0, 1, (k > 1 && slabs_supported(s->d)) ? (k > CG_MAX_SLABS ? CG_MAX_SLABS : k) : 1, 0};
@@ -1592,7 +1589,7 @@ extern "C" int cg_solver_set_slabs(cg_solver* s, int slabs) {
 extern "C" int cg_solver_set_zstaging(cg_solver* s, int tma) {
   CG_REQUIRE(s, "null solver");
   CG_REQUIRE(tma == 0 || tma == 1, "tma must be 0 or 1, got %d", tma);
-  CG_REQUIRE(!tma || s->ztma_dev,
+  CG_REQUIRE(!tma || s->ztma_ok,
              "tensor-map staging needs persistent z-passes with nz / 2 + 1 <= 256 and an even ny (grid %dx%dx%d)",
              s->d.nx, s->d.ny, s->d.nz);
   CG_REQUIRE(!tma || s->slabs == 1, "tensor-map staging runs the plain step only (slabs = %d)", s->slabs);

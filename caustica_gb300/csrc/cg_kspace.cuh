@@ -128,9 +128,9 @@ bool fast_zpass_p(int mode, const Dims& d, const Tables& t, const MediumDev& m, 
 // Tensor-map (TMA) staging of the persistent z-tiles: one descriptor per
 // spectrum in the u-pass's component order (S1, S0, S2; the p-pass reads
 // map[1] = S0), each a [member x][kz][2 ny floats] grid of 32-float x kz
-// boxes, and a device flag that a staging wait sets if it gives up. The
-// kernels read the descriptors from global memory (written once by the host
-// before any launch that uses them).
+// boxes, and a device flag that a staging wait sets if it gives up. Kernels
+// take the whole struct by value as a __grid_constant__ parameter, so every
+// launch carries its own copy of the descriptors.
 struct ZTma {
   CUtensorMap map[3];
   int* err;
@@ -141,13 +141,13 @@ int ztma_supported(const Dims& d);
 // Encode the three descriptors for `batch` members into *z (host memory);
 // CG_OK, or an error (set) when the driver refuses them.
 int ztma_encode(ZTma* z, const Dims& d, int batch, float2* S1, float2* S0, float2* S2);
-// u- and p-passes staged by tensor map (persistent kernels; z_dev: the
-// descriptors in device memory). False when the grid has no such kernel.
+// u- and p-passes staged by tensor map (persistent kernels; z: the encoded
+// descriptors, host memory). False when the grid has no such kernel.
 bool fast_zpass_u_tma(const Dims& d, const Tables& t, const MediumDev& m, float* u, float2* S0, float2* S1,
-                      float2* S2, int batch, cudaStream_t st, const ZTma* z_dev);
+                      float2* S2, int batch, cudaStream_t st, const ZTma& z);
 bool fast_zpass_p_tma(const Dims& d, const Tables& t, const MediumDev& m, const SourceDev& src, const RecordDev& rec,
                       const long long* ctl, int n_local, int record, float* p, float2* S0, int batch,
-                      cudaStream_t st, const ZTma* z_dev);
+                      cudaStream_t st, const ZTma& z);
 
 // The forward z-transform of p into S0 with the kernel family the step's
 // p-pass runs on this grid (bitwise the spectrum a step leaves); false when

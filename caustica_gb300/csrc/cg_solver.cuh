@@ -44,10 +44,12 @@ struct cg_solver {
   // each slab's spectra and fields stay in L2 between its three passes; the
   // pressure spectrum between steps is then y- and z-transformed
   int slabs = 1;
-  // tensor-map staging of the persistent z-tiles: descriptors of S1, S0, S2
-  // in device memory (null where the grid does not allow it), the flag a
-  // staging wait raises when it gives up, and whether the step uses it
-  ZTma* ztma_dev = nullptr;
+  // tensor-map staging of the persistent z-tiles: the encoded descriptors of
+  // S1, S0, S2 (host memory; each launch passes them by value) with the
+  // device flag a staging wait raises when it gives up, whether they exist
+  // on this grid, and whether the step uses them
+  ZTma ztma_host = {};
+  int ztma_ok = 0;
   int* ztma_err = nullptr;
   int ztma = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one period, record off/on
