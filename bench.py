@@ -301,6 +301,7 @@ def run_gb300(args, dist, rank, ws, local):
     dev = eng.DeviceSolver(plan)
     launches_per_step = dev.launches_per_step
     tuning = dev.tuning
+    staging_tma = dev.config()["tma_staging"]  # the staging in effect (also without the autotuner)
     try:
         # drive table long enough that the source keeps injecting through the timed steps
         dev.extend_drive((plan.eff_min + 4) * plan.spp + W + 2 * K)
@@ -333,8 +334,7 @@ def run_gb300(args, dist, rank, ws, local):
     dom = int(np.argmax(per_launch_ms))
     achieved = bytes_slot[dom] / (per_launch_ms[dom] * 1e-3) / 1e9
     kernel_name = SLOTS[dom]
-    symbols = slot_symbols(plan.padded3, bool((tuning or {}).get("persistent_z", True)),
-                           bool((tuning or {}).get("tma_staging", False)))
+    symbols = slot_symbols(plan.padded3, bool((tuning or {}).get("persistent_z", True)), bool(staging_tma))
     traffic = _traffic_from_profiles(kernel_name)
     step_b = step_algorithmic_bytes(info_labels, True)
     step_achieved = step_b * value / ws / 1e9
