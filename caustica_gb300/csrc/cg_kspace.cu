@@ -842,6 +842,7 @@ extern "C" int cg_solver_create(const cg_solver_config* cfg, cg_solver** out) {
       }
     }
     cudaGetLastError();
+    if (!s->ztma_ok) cg_set_error("%s", "");  // a refused descriptor is not an error of the create call
   }
   cudaStream_t st = s->stream;
   k_twiddles<<<(cfg->nx + 255) / 256, 256, 0, st>>>(s->twx, cfg->nx);
