@@ -84,3 +84,39 @@ def test_the_tuner_reports_its_staging_choice():
     with DeviceSolver(plan) as dev:
         assert isinstance(dev.tuning["tma_staging"], bool)
         assert dev.tuning["tma_staging"] == dev.config()["tma_staging"]
+
+
+def test_handles_created_and_destroyed_from_several_threads_stay_bitwise():
+    """Handles of different grids come and go concurrently (as in a serving
+    process), so a new handle's staging can follow a freed one's on the same
+    device: every tensor-map-staged run must still equal its cp.async run."""
+    import threading
+
+    plans = [_case(shape, nl, seed=40 + i) for i, (shape, nl) in
+             enumerate([((16, 32, 64), False), ((12, 40, 128), True), ((10, 34, 320), False)])]
+
+    def run(plan, tma):
+        with DeviceSolver(plan, autotune=False) as dev:
+            dev.set_zstaging(tma)
+            dev.run_periods(1)
+            return dev.get_state()[0], dev.read_peaks(0, 1)
+
+    want = [run(p, False) for p in plans]
+    errors = []
+
+    def worker(k):
+        try:
+            for r in range(6):
+                i = (k + r) % len(plans)
+                p, peaks = run(plans[i], True)
+                np.testing.assert_array_equal(p, want[i][0])
+                np.testing.assert_array_equal(peaks, want[i][1])
+        except Exception as exc:  # noqa: BLE001 - reported below
+            errors.append(exc)
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
